@@ -1,0 +1,352 @@
+"""Benchmark of the Wilson-loop <W> hot path on GB300 (one JSON line).
+
+Workload (spinor-QED <W> of one isolated smooth flux tube): profile
+f = rho^2/(lambda^2 + rho^2), lambda = 1, flux F in {0.1, 1, 10} sharing one
+geometric pass; Nl = 5120 unit loops of ppl = 2048 points (float32
+[Nl][ppl][4], seed 2, generated on the device); 128 log-spaced T in
+[1e-3, 1e3]; 64 rho uniform in [0, 8]; Simpson with 5 nodes (4 intervals) per
+segment; FP32 phases with compensated sums, FP64 loop averages, groups of 128
+loops.  One step = one pass over all 8192 (rho, T) instances:
+5120 * 2048 * 8192 = 8.59e10 loop-segments.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value : loop-segments/s with the ensemble resident in HBM (wl_eval_device,
+        CUDA events on the library's stream; 160 MiB ensemble > L2).
+e2e   : the same metric through wl_ensemble_upload + wl_eval + release with
+        host buffers (host->device copy of the ensemble and instances, and
+        device->host copy of every group result inside the timed region).
+--impl reference : the reference's Wilson-loop formula as C (the FP32 port
+        of intEV.cu:408-571 + Integrand.c:325-407) on all host cores, on a
+        bounded sample of the same workload.
+Under torchrun every rank evaluates the full workload on its own GPU (weak
+scaling, no data-path collective); times are the max over ranks (gloo).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "worldline-flux-tube-lattice_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "loop-segments/s"
+NL, PPL, SEED = 5120, 2048, 2
+NT, NRHO = 128, 64
+FLUX = [0.1, 1.0, 10.0]
+NINT = 4
+GROUP = 128
+# FP32 and MUFU operations per loop-segment of the smooth spinor kernel at 5
+# nodes, counted from the source (segment() in csrc/wl_device.cuh): point
+# transform 2, setup 8, clamps 3, end value 4, 3 interior rho^2 x 3, 5 nodes
+# x (add + square), Simpson sums 6 + 8 combines -> 52 FP32; 5 reciprocals.
+ALG_FP32_PER_SEG = 52
+ALG_MUFU_PER_SEG = 5
+# loop data a segment reads (one float4 point) -- HBM side of the roofline
+ALG_BYTES_PER_POINT = 16
+
+
+def workload():
+    T = np.geomspace(1e-3, 1e3, NT)
+    rho = np.linspace(0.0, 8.0, NRHO)
+    cx = np.repeat(rho, NT)
+    T = np.tile(T, NRHO)
+    cy = np.zeros_like(cx)
+    return cx, cy, T
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(seconds_target=12.0, threads=0):
+    """The FP32 C port of the reference's per-loop formula and EVMean on all
+    host cores, timed on a bounded sample of the workload."""
+    from oracle import oracle
+
+    cx, cy, T = workload()
+    rng = np.random.default_rng(0)
+    loops = oracle.vloops(SEED, 128, PPL)
+    fld = oracle.field("smooth", fermion=1, nint=NINT)
+    # calibrate on a small slice, then size the sample for ~seconds_target
+    idx = rng.choice(len(T), 16, replace=False)
+    t0 = time.perf_counter()
+    oracle.eval_groups(loops[:128], cx[idx], cy[idx], T[idx], FLUX, fld, group=128,
+                       fp32=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    rate = 16 * 128 * PPL / dt
+    n = int(max(16, min(len(T), seconds_target * rate / (128 * PPL))))
+    idx = rng.choice(len(T), n, replace=False)
+    t0 = time.perf_counter()
+    oracle.eval_groups(loops[:128], cx[idx], cy[idx], T[idx], FLUX, fld, group=128,
+                       fp32=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    segs = n * 128 * PPL
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return segs / dt, cores, "%d loops x %d points x %d (rho,T) instances (3 F each), %.1f s" % (
+        128, PPL, n, dt)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(seconds_target=2.0)
+    info = None
+    for _ in range(args.steps):
+        v, cores, sample = cpu_sample(seconds_target=args.cpu_seconds)
+        vals.append(v)
+        info = (cores, sample)
+    value = float(np.median(vals))
+    segs_step = NL * PPL * NT * NRHO
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "segments/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": segs_step / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_dict(),
+        "cpu_baseline": {"value": value, "unit": "segments/s", "cores": info[0], "kind": "port",
+                         "sample": info[1]},
+        "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def config_dict():
+    return {"workload": "spinor-QED <W>, smooth flux tube lambda=1, F in {0.1,1,10} on one "
+                        "geometric pass, Nl=5120 x ppl=2048 (seed 2), 128 log T in [1e-3,1e3] "
+                        "x 64 rho in [0,8], Simpson 5 nodes, ref-compat clamps, groups of 128",
+            "Nl": NL, "ppl": PPL, "instances": NT * NRHO, "flux_values": len(FLUX),
+            "simpson_nodes": NINT + 1, "segments_per_step": NL * PPL * NT * NRHO,
+            "l2": "inputs larger than L2 (160 MiB ensemble), no flush"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+
+    import wltube
+
+    torch.cuda.set_device(local)
+    ctx = wltube.Context(local)
+    fld = wltube.field("smooth", fermion=1, nint=NINT)
+    cx, cy, T = workload()
+    ninst = len(T)
+    h = ctx.generate(SEED, NL, PPL)
+    dcx = torch.tensor(cx, dtype=torch.float64, device="cuda")
+    dcy = torch.tensor(cy, dtype=torch.float64, device="cuda")
+    dT = torch.tensor(T, dtype=torch.float64, device="cuda")
+    ng = NL // GROUP
+    dgrp = torch.empty(ninst * len(FLUX) * ng, dtype=torch.float64, device="cuda")
+    dmean = torch.empty(ninst * len(FLUX), dtype=torch.float64, device="cuda")
+    dsem = torch.empty_like(dmean)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    def step():
+        ctx.eval_device(h, fld, ninst, dcx.data_ptr(), dcy.data_ptr(), dT.data_ptr(), FLUX,
+                        GROUP, dgrp.data_ptr(), dmean.data_ptr(), dsem.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    # ---- device-resident timed region ------------------------------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    t1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    per_launch_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    segs_step = NL * PPL * ninst
+    ms_step = total_ms / args.steps
+    value = world * segs_step / (ms_step * 1e-3)
+    launches = 3 * args.steps
+    # ---- roofline: FP32 issue bound; peaks measured here ------------------
+    fp32_peak = ctx.peak_probe(0)
+    mufu_peak = ctx.peak_probe(1)
+    seg_rate = segs_step / (per_launch_ms * 1e-3)
+    fp32_ach = seg_rate * ALG_FP32_PER_SEG
+    mufu_ach = seg_rate * ALG_MUFU_PER_SEG
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        hbm_peak = 6800.0
+    hbm_ach = NL * PPL * ALG_BYTES_PER_POINT / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))[
+            "dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        pass
+    # ---- end to end through the C ABI with host buffers --------------------
+    e2e = None
+    if not args.no_e2e:
+        host_loops = ctx.download(h)
+        groups = np.empty((ninst, len(FLUX), ng))
+        mean = np.empty((ninst, len(FLUX)))
+        sem = np.empty((ninst, len(FLUX)))
+        import ctypes as C
+
+        L = wltube.lib()
+
+        def e2e_step():
+            hh = ctx.upload(host_loops)
+            ctx._check(L.wl_eval(ctx.handle, hh, C.byref(fld), ninst,
+                                 wltube._p(cx, C.c_double), wltube._p(cy, C.c_double),
+                                 wltube._p(T, C.c_double), len(FLUX),
+                                 wltube._p(np.array(FLUX), C.c_double), GROUP,
+                                 wltube._p(groups, C.c_double), wltube._p(mean, C.c_double),
+                                 wltube._p(sem, C.c_double)))
+            ctx.release(hh)
+
+        e2e_step()
+        barrier(world)
+        s0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = max_over_ranks(time.perf_counter() - s0, world)
+        e2e = {"value": world * segs_step * args.steps / e2e_s, "unit": "segments/s",
+               "h2d_bytes_per_step": int(host_loops.nbytes + 3 * 8 * ninst),
+               "d2h_bytes_per_step": int(groups.nbytes + mean.nbytes + sem.nbytes)}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, sample = cpu_sample(seconds_target=args.cpu_seconds)
+        cpu = {"value": v, "unit": "segments/s", "cores": cores, "kind": "port",
+               "sample": sample}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: device-generated seeded unit loops (Philox4x32-10, seed 2)",
+        "config": config_dict(),
+        "W_evals_per_s": world * ninst * len(FLUX) / (ms_step * 1e-3),
+        "roofline": {
+            "bound": "fp32", "unit": "Gop/s",
+            "achieved": fp32_ach / 1e9, "peak": fp32_peak / 1e9, "frac": fp32_ach / fp32_peak,
+            "traffic": traffic,
+            "peak_source": "FP32 FMA-chain probe measured in this run (no FP32 peak in "
+                           "MEASURED_PEAKS.json)",
+            "alg_ops_per_segment": {"fp32": ALG_FP32_PER_SEG, "mufu": ALG_MUFU_PER_SEG},
+            "mufu": {"achieved": mufu_ach / 1e9, "peak": mufu_peak / 1e9,
+                     "frac": mufu_ach / mufu_peak},
+            "hbm": {"achieved_gbs": hbm_ach, "peak_gbs": hbm_peak,
+                    "frac": hbm_ach / hbm_peak if hbm_peak else None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+            "kernel_ms": per_launch_ms,
+        },
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(line))
+    ctx.release(h)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

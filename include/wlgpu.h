@@ -1,0 +1,154 @@
+/*
+ * wlgpu.h -- C ABI of the GB300 Wilson-loop library (libwlgpu.so).
+ *
+ * Replaces the reference's kernel boundary (intEV.cu:111-148, intEVff.cu:96-131:
+ * EV() launching ExpectValue and averaging with EVMean, Integrand.c:325-407)
+ * with (1) the same legacy entry point EV() (declared in wl_legacy.h) and
+ * (2) a status-returning batched API that evaluates many (centre of mass,
+ * proper time, flux) instances of one field profile in one pass over a
+ * device-resident loop ensemble.
+ *
+ * Conventions
+ *  - Every function returns WL_OK (0) or a negative WL_ERR_* status; the
+ *    message of the last failure is available from wl_last_error().
+ *  - Pointers named host_* are host memory; the library copies them.  Device
+ *    pointers are named dev_* .  Nothing is retained after a call returns
+ *    unless stated (ensembles).
+ *  - A context owns one CUDA stream on one device; calls on one context must
+ *    not run concurrently from several host threads.
+ *  - Loop ensembles are float32 [Nl][ppl][4] (x, y, z, w), the reference's
+ *    float4 layout (EffAct.c:368-381); only x and y enter the Wilson loop.
+ *    ppl must be a multiple of 4 (sub-loop structure, intEV.cu:461-506).
+ */
+#ifndef WLGPU_H
+#define WLGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WL_OK 0
+#define WL_ERR_INVALID (-1) /* an argument is out of range                 */
+#define WL_ERR_CUDA (-2)    /* a CUDA runtime call failed                   */
+#define WL_ERR_NOMEM (-3)   /* device or pinned host allocation failed      */
+#define WL_ERR_TIMEOUT (-4) /* a bounded device-side wait gave up           */
+#define WL_ERR_NOTFOUND (-5)/* unknown ensemble handle                      */
+#define WL_ERR_ADMISSION (-6)/* request exceeds the admission budget        */
+
+/* field profiles: the values of the reference's profile macros (intT.h) */
+#define WL_PROFILE_STEP 0
+#define WL_PROFILE_SMOOTH 1
+#define WL_PROFILE_QUADRATIC 2
+#define WL_PROFILE_GAUSSIAN 3
+#define WL_PROFILE_PERIODIC 4
+#define WL_PROFILE_FIXFLUX 6
+
+/* clamp modes of the segment polynomial */
+#define WL_MODE_REFCOMPAT 0 /* the reference's clamps (intEV.cu:418-422, 439) */
+#define WL_MODE_EXACT 1     /* exact rho^2(t); 1e-30 floor where f/rho^2 divides */
+
+/* flux-tube field and quadrature of one evaluation */
+typedef struct {
+  int profile;    /* WL_PROFILE_*                                             */
+  int fermion;    /* 1: spinor QED (spin factor cosh), 0: scalar QED          */
+  int nint;       /* Simpson intervals per segment, even, 2..64 (ref: 50)     */
+  int mode;       /* WL_MODE_*                                                */
+  int ff_variant; /* fixflux: 0 = intEV.cu phi/chi fits, 1 = intEVff.cu ones  */
+  int reserved;
+  double lambda2; /* lambda^2                                                 */
+  double tubedist;/* lattice spacing a (periodic, fixflux)                    */
+  double lmin;    /* fixflux minimum width (0.1 a in the reference)           */
+} wl_field;
+
+typedef struct wl_ctx wl_ctx;
+
+/* version and status text */
+const char *wl_version(void);
+const char *wl_status_string(int status);
+
+/* context: one device, one stream */
+int wl_ctx_create(int device, wl_ctx **out);
+int wl_ctx_destroy(wl_ctx *ctx);
+int wl_last_error(wl_ctx *ctx, char *buf, int buflen);
+int wl_ctx_synchronize(wl_ctx *ctx);
+
+/* ---- resident loop ensembles ------------------------------------------ */
+/* copy a host ensemble to the device; *handle identifies it afterwards */
+int wl_ensemble_upload(wl_ctx *ctx, const float *host_loops, int Nl, int ppl,
+                       int *handle);
+/* use caller-owned device memory (not freed by the library) */
+int wl_ensemble_wrap(wl_ctx *ctx, const float *dev_loops, int Nl, int ppl,
+                     int *handle);
+/* generate seeded unit loops on the device: closed Brownian bridges of unit
+ * proper time, per-component step variance 2/ppl, centre of mass at the
+ * origin; loop l draws Philox4x32-10 numbers keyed by (seed, first + l). */
+int wl_ensemble_generate(wl_ctx *ctx, uint64_t seed, int first, int Nl, int ppl,
+                         int *handle);
+int wl_ensemble_download(wl_ctx *ctx, int handle, float *host_loops);
+int wl_ensemble_release(wl_ctx *ctx, int handle);
+/* device pointer and sizes of an ensemble */
+int wl_ensemble_info(wl_ctx *ctx, int handle, const float **dev_loops, int *Nl,
+                     int *ppl);
+
+/* ---- batched <W> -------------------------------------------------------- */
+/* Evaluate ninst instances (host_cx[i], host_cy[i], host_T[i]) for each of the
+ * nF flux values host_F[j] (nF <= 4) on ensemble `handle`, with loops split
+ * into ng = Nl / group groups (Nl % group == 0; the reference uses 128).
+ * Outputs (host, any may be NULL):
+ *   out_group[(i*nF + j)*ng + g]  <W> of group g, Richardson-combined
+ *                                 8/3 W_N - 2 W_N/2 + 1/3 W_N/4
+ *                                 (Integrand.c:352-400)
+ *   out_mean[i*nF + j]            mean over groups
+ *   out_sem[i*nF + j]             standard error of that mean over groups
+ * The per-loop phases are FP32 (compensated sums); the loop averages FP64.  */
+int wl_eval(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
+            const double *host_cx, const double *host_cy, const double *host_T,
+            int nF, const double *host_F, int group, double *out_group,
+            double *out_mean, double *out_sem);
+
+/* Asynchronous variant on the context's stream for device-resident inputs and
+ * outputs: dev_cx, dev_cy, dev_T [ninst] and the outputs are device pointers
+ * (FP64, same layouts as wl_eval; outputs may be NULL), host_F stays a host
+ * array.  Nothing is synchronised; invalid instances (T <= 0 or not finite)
+ * and device-side wait time-outs are reported by the next
+ * wl_ctx_synchronize().  Three kernel launches: instance set-up, sweep,
+ * reduction. */
+int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
+                   const double *dev_cx, const double *dev_cy, const double *dev_T,
+                   int nF, const double *host_F, int group, double *dev_out_group,
+                   double *dev_out_mean, double *dev_out_sem);
+
+/* Throughput probe of one SM pipe on the context's device, for roofline
+ * denominators: kind 0 = FP32 FMA, 1 = MUFU reciprocal.  *ops_per_s receives
+ * lane operations per second over the whole device (about 0.1 s of work). */
+int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s);
+
+/* the context's CUDA stream (a cudaStream_t), for timing and interop */
+int wl_ctx_stream(wl_ctx *ctx, void **stream);
+
+/* Per-loop outputs of one instance, the reference kernel's Wsscal/Wsferm
+ * (intEV.cu:553-561): host_scal[l*4 + k], host_ferm[l*4 + k], k = 0 (N/2),
+ * 1 (N/4, i = 2 mod 4), 2 (N/4, i = 0 mod 4), 3 unused (0). */
+int wl_loops(wl_ctx *ctx, int handle, const wl_field *field, double cx, double cy,
+             double T, double F, float *host_scal, float *host_ferm);
+
+/* How the last wl_eval on this context was run: kernel launches issued and
+ * which sweep kernel ("instance-parallel" or "loop-parallel"). */
+int wl_last_launches(wl_ctx *ctx, int *launches, const char **sweep_kind);
+
+/* ---- legacy EV() configuration ----------------------------------------- */
+/* The reference selects the profile at compile time (intT.h "profile"); the
+ * library's EV() uses the profile, lattice spacing, Simpson intervals and
+ * clamp mode set here (default: smooth, a = 1, 50 intervals, ref-compat).   */
+int wl_legacy_configure(int profile, double tubedist, double lmin, int nint,
+                        int mode);
+/* the configuration EV() uses (any pointer may be NULL) */
+int wl_legacy_query(int *profile, double *tubedist, double *lmin, int *nint, int *mode);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WLGPU_H */

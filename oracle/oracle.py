@@ -1,0 +1,229 @@
+"""ctypes front end of the CPU oracle (oracle/wl_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the
+CPU-baseline leg of bench.py.  The product library never imports it.
+
+The C library is built by ``build()`` below (called from
+``__graft_entry__.build()``) into ``oracle/liboracle.so``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+PROFILES = {"step": 0, "smooth": 1, "quadratic": 2, "gaussian": 3,
+            "periodic": 4, "spline": 5, "fixflux": 6}
+REFCOMPAT, EXACT = 0, 1
+QED_M2, QED_E = 1.0, 0.30282212  # Integrand.c:12-14
+
+
+class Field(C.Structure):
+    """wlo_field of wl_oracle.h."""
+    _fields_ = [("profile", C.c_int), ("fermion", C.c_int), ("nint", C.c_int),
+                ("mode", C.c_int), ("ff_variant", C.c_int), ("pad_", C.c_int),
+                ("lambda2", C.c_double), ("tubedist", C.c_double),
+                ("lmin", C.c_double)]
+
+
+class Qed(C.Structure):
+    _fields_ = [("m2", C.c_double), ("e", C.c_double)]
+
+
+def field(profile="smooth", fermion=0, nint=50, mode=REFCOMPAT, lambda2=1.0,
+          tubedist=1.0, lmin=None, ff_variant=0) -> Field:
+    if isinstance(profile, str):
+        profile = PROFILES[profile]
+    if lmin is None:
+        lmin = 0.1 * tubedist
+    return Field(profile, fermion, nint, mode, ff_variant, 0, lambda2, tubedist, lmin)
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "wl_oracle.c")
+    deps = [src, os.path.join(HERE, "wl_oracle_body.h"), os.path.join(HERE, "wl_oracle.h")]
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(d) for d in deps)):
+        return LIB_PATH
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp",
+                           "-ffp-contract=off", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        dp, fp, ip = C.POINTER(C.c_double), C.POINTER(C.c_float), C.POINTER(C.c_int)
+        Fp = C.POINTER(Field)
+        L.wlo64_flambda.restype = C.c_double
+        L.wlo64_flambda.argtypes = [C.c_double, Fp]
+        L.wlo64_fplambda.restype = C.c_double
+        L.wlo64_fplambda.argtypes = [C.c_double, Fp]
+        L.wlo64_fl_over_rho2.restype = C.c_double
+        L.wlo64_fl_over_rho2.argtypes = [C.c_double, Fp]
+        L.wlo64_idt.argtypes = [C.c_double, C.c_double, C.c_double, Fp, dp, dp]
+        L.wlo64_loop_sums.argtypes = [fp, C.c_int, C.c_double, C.c_double, C.c_double,
+                                      Fp, dp, dp]
+        L.wlo32_loop_sums.argtypes = [fp, C.c_int, C.c_float, C.c_float, C.c_float,
+                                      Fp, fp, fp]
+        L.wlo64_loops.argtypes = [fp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, Fp, dp, dp]
+        L.wlo64_wfactors.argtypes = [dp, dp, C.c_int, dp]
+        L.wlo64_evmean.restype = C.c_double
+        L.wlo64_evmean.argtypes = [dp, dp, C.c_int, ip, C.c_int]
+        for name in ("wlo64_eval", "wlo32_eval"):
+            getattr(L, name).argtypes = [fp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.c_int,
+                                         dp, Fp, C.c_int, dp, C.c_int]
+        Qp = C.POINTER(Qed)
+        L.wlo_magfield.restype = C.c_double
+        L.wlo_magfield.argtypes = [C.c_double, C.c_double, Fp, Qp]
+        L.wlo_exact.restype = C.c_double
+        L.wlo_exact.argtypes = [C.c_double, C.c_double, C.c_int, Qp]
+        L.wlo_smTscal.restype = C.c_double
+        L.wlo_smTscal.argtypes = [C.c_double, C.c_double, Qp]
+        L.wlo_smTferm.restype = C.c_double
+        L.wlo_smTferm.argtypes = [C.c_double, C.c_double, Qp]
+        L.wlo_tfunc_regime.restype = C.c_int
+        L.wlo_tfunc_regime.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, Fp,
+                                       Qp, dp]
+        L.wlo_tfunc_mc.restype = C.c_double
+        L.wlo_tfunc_mc.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, Fp, Qp]
+        L.wlo64_integrateT.argtypes = [fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                       C.c_double, C.c_double, Fp, Qp, dp, dp, dp, C.c_int]
+        u32p = C.POINTER(C.c_uint32)
+        L.wlo_philox4x32.argtypes = [u32p, u32p, u32p]
+        L.wlo_vloops.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, fp]
+        _lib = L
+    return _lib
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+QED = Qed(QED_M2, QED_E)
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().wlo_philox4x32(c, k, o)
+    return list(o)
+
+
+def vloops(seed: int, Nl: int, ppl: int, first: int = 0) -> np.ndarray:
+    """Seeded unit loops, float32 [Nl][ppl][4]."""
+    out = np.empty((Nl, ppl, 4), dtype=np.float32)
+    lib().wlo_vloops(seed, first, Nl, ppl, _ptr(out, C.c_float))
+    return out
+
+
+def loop_sums(loop, cx, cy, rtT, fld, fp32=False):
+    loop = _f(loop)
+    if fp32:
+        gs, gf = (C.c_float * 3)(), (C.c_float * 3)()
+        lib().wlo32_loop_sums(_ptr(loop, C.c_float), loop.shape[0], cx, cy, rtT,
+                              C.byref(fld), gs, gf)
+    else:
+        gs, gf = (C.c_double * 3)(), (C.c_double * 3)()
+        lib().wlo64_loop_sums(_ptr(loop, C.c_float), loop.shape[0], cx, cy, rtT,
+                              C.byref(fld), gs, gf)
+    return np.array(list(gs)), np.array(list(gf))
+
+
+def loops_phases(loops, cx, cy, T, F, fld):
+    """Per-loop Wsscal / Wsferm (FP64), each [Nl][3] in (x, y, z) order."""
+    loops = _f(loops)
+    Nl, ppl = loops.shape[:2]
+    s = np.empty((Nl, 3))
+    f = np.empty((Nl, 3))
+    lib().wlo64_loops(_ptr(loops, C.c_float), Nl, ppl, cx, cy, T, F, C.byref(fld),
+                      _ptr(s, C.c_double), _ptr(f, C.c_double))
+    return s, f
+
+
+def wfactors(scal, ferm, fermion):
+    s, f = _d(scal), _d(ferm)
+    w = np.empty(3)
+    lib().wlo64_wfactors(_ptr(s, C.c_double), _ptr(f, C.c_double), fermion,
+                         _ptr(w, C.c_double))
+    return w
+
+
+def evmean(scal, ferm, WL, fermion):
+    s, f = _d(scal), _d(ferm)
+    wl = np.ascontiguousarray(WL, dtype=np.int32)
+    return lib().wlo64_evmean(_ptr(s, C.c_double), _ptr(f, C.c_double), len(wl),
+                              _ptr(wl, C.c_int), fermion)
+
+
+def eval_groups(loops, cx, cy, T, F, fld, group=128, fp32=False, nthreads=0):
+    """Per-group <W>: array [ninst][nF][Nl//group]."""
+    loops = _f(loops)
+    Nl, ppl = loops.shape[:2]
+    cx, cy, T, F = _d(np.atleast_1d(cx)), _d(np.atleast_1d(cy)), _d(np.atleast_1d(T)), \
+        _d(np.atleast_1d(F))
+    n = len(T)
+    ng = Nl // group
+    out = np.empty((n, len(F), ng))
+    fn = lib().wlo32_eval if fp32 else lib().wlo64_eval
+    fn(_ptr(loops, C.c_float), Nl, ppl, n, _ptr(cx, C.c_double), _ptr(cy, C.c_double),
+       _ptr(T, C.c_double), len(F), _ptr(F, C.c_double), C.byref(fld), group,
+       _ptr(out, C.c_double), nthreads)
+    return out
+
+
+def magfield(rho2, F, fld):
+    return lib().wlo_magfield(rho2, F, C.byref(fld), C.byref(QED))
+
+
+def exact(T, B, fermion):
+    return lib().wlo_exact(T, B, fermion, C.byref(QED))
+
+
+def smT(B, T, fermion):
+    return (lib().wlo_smTferm if fermion else lib().wlo_smTscal)(B, T, C.byref(QED))
+
+
+def tfunc_regime(T, cx, cy, F, fld):
+    v = C.c_double()
+    r = lib().wlo_tfunc_regime(T, cx, cy, F, C.byref(fld), C.byref(QED), C.byref(v))
+    return r, v.value
+
+
+def tfunc_mc(T, EVg, cx, cy, F, fld):
+    return lib().wlo_tfunc_mc(T, EVg, cx, cy, F, C.byref(fld), C.byref(QED))
+
+
+def integrateT(loops, n, cx, cy, F, fld, nthreads=0):
+    loops = _f(loops)
+    Nl, ppl = loops.shape[:2]
+    ng = Nl // 128
+    val = np.empty(ng)
+    leff, sem = C.c_double(), C.c_double()
+    lib().wlo64_integrateT(_ptr(loops, C.c_float), Nl, ppl, n, ng, cx, cy, F, C.byref(fld),
+                           C.byref(QED), _ptr(val, C.c_double), C.byref(leff), C.byref(sem),
+                           nthreads)
+    return val, leff.value, sem.value

@@ -1,0 +1,212 @@
+"""GPU parity: libwlgpu.so through its C ABI against the FP64 oracle and the
+reference's own outputs.
+
+Tolerances (stated once, used throughout):
+  PHASE_TOL  per-loop phases / spin exponents, relative to the largest value
+             of the case: FP32 kernel vs FP64 oracle (the reference kernel
+             itself is FP32 with approximate divides).
+  W_TOL      <W> per group: |W - W64| / max(|W64|, W_FLOOR) <= 1e-5, the
+             spec tolerance; the floor keeps the metric meaningful when
+             <W> is small (loop averages of O(1) cosines cancel).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PHASE_TOL = 2e-5
+W_TOL = 1e-5
+W_FLOOR = 1e-2
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "golden_ref.npz")
+
+
+@pytest.fixture(scope="module")
+def wl():
+    import wltube
+
+    wltube.lib()
+    return wltube
+
+
+@pytest.fixture(scope="module")
+def ctx(wl):
+    c = wl.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def gold():
+    z = np.load(GOLD)
+    return z, json.loads(bytes(z["meta"]).decode())
+
+
+def werr(w, ref):
+    return np.max(np.abs(w - ref) / np.maximum(np.abs(ref), W_FLOOR))
+
+
+def test_generator_matches_oracle(ctx):
+    h = ctx.generate(seed=3, Nl=64, ppl=256, first=5)
+    dev = ctx.download(h)
+    ctx.release(h)
+    host = O.vloops(3, 64, 256, first=5)
+    assert np.abs(dev - host).max() < 2e-6
+    # closed bridge with the centre of mass at the origin
+    assert np.abs(dev.mean(axis=1)).max() < 1e-5
+
+
+def test_per_loop_phases_match_reference_golden(ctx, wl, gold):
+    z, meta = gold
+    h = ctx.upload(z["loops"])
+    try:
+        for case, ref in zip(meta["LOOP_CASES"], z["loop_out"]):
+            _d, prof, ffv, fe, l2, cx, cy, T, F, a = case
+            fld = wl.field(prof, fermion=fe, nint=50, lambda2=l2, tubedist=a, ff_variant=ffv)
+            s, f = ctx.loops(h, fld, cx, cy, T, F)
+            scale = max(np.abs(ref[:, :3]).max(), 1e-30)
+            assert np.abs(s[:, :3] - ref[:, :3]).max() / scale < PHASE_TOL, case
+            if fe:
+                fscale = max(np.abs(ref[:, 4:7]).max(), 1e-30)
+                assert np.abs(f[:, :3] - ref[:, 4:7]).max() / fscale < PHASE_TOL, case
+    finally:
+        ctx.release(h)
+
+
+@pytest.mark.parametrize("nint", [4, 50, 8])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_per_loop_phases_match_oracle(ctx, wl, nint, mode):
+    loops = O.vloops(21, 128, 128)
+    h = ctx.upload(loops)
+    try:
+        for prof, fe, l2, cx, T, F in [("smooth", 1, 1.0, 0.5, 1.0, 1.0),
+                                       ("gaussian", 1, 0.5, 1.2, 0.3, 2.0),
+                                       ("step", 0, 2.0, 0.2, 0.7, 1.0),
+                                       ("quadratic", 1, 1.5, 0.0, 0.2, 1.0)]:
+            fld = wl.field(prof, fermion=fe, nint=nint, mode=mode, lambda2=l2)
+            s, f = ctx.loops(h, fld, cx, 0.0, T, F)
+            os_, of = O.loops_phases(loops, cx, 0.0, T, F,
+                                     O.field(prof, fermion=fe, nint=nint, mode=mode, lambda2=l2))
+            assert np.abs(s[:, :3] - os_).max() / np.abs(os_).max() < PHASE_TOL, (prof, nint)
+            if fe:
+                assert np.abs(f[:, :3] - of).max() / np.abs(of).max() < PHASE_TOL, (prof, nint)
+    finally:
+        ctx.release(h)
+
+
+def _instances(n, rho_max, Tlo, Thi, seed):
+    rng = np.random.default_rng(seed)
+    cx = rng.uniform(0.0, rho_max, n)
+    cy = rng.uniform(-0.2, 0.2, n)
+    T = np.exp(rng.uniform(np.log(Tlo), np.log(Thi), n))
+    return cx, cy, T
+
+
+@pytest.mark.parametrize("prof,fe,nint,l2", [("smooth", 0, 4, 1.0), ("smooth", 1, 4, 1.0),
+                                             ("smooth", 1, 50, 1.0), ("gaussian", 1, 4, 1.0),
+                                             ("step", 1, 4, 2.0), ("quadratic", 0, 8, 1.0)])
+def test_batched_eval_matches_oracle(ctx, wl, prof, fe, nint, l2):
+    loops = O.vloops(2, 256, 256)
+    cx, cy, T = _instances(160, 3.0, 0.01, 10.0, 7)
+    F = [0.1, 1.0, 3.0]
+    h = ctx.upload(loops)
+    try:
+        g, mean, sem = ctx.eval(h, wl.field(prof, fermion=fe, nint=nint, lambda2=l2),
+                                cx, cy, T, F, group=128)
+        assert ctx.last_launches()[1] == "instance-parallel"
+    finally:
+        ctx.release(h)
+    ref = O.eval_groups(loops, cx, cy, T, F, O.field(prof, fermion=fe, nint=nint, lambda2=l2))
+    assert werr(g, ref) < W_TOL
+    np.testing.assert_allclose(mean, ref.mean(axis=2), rtol=0, atol=W_TOL * 10)
+
+
+def test_loop_parallel_eval_matches_oracle(ctx, wl):
+    loops = O.vloops(4, 512, 64)
+    cx, cy, T = _instances(5, 2.0, 0.05, 5.0, 11)
+    fld = wl.field("smooth", fermion=1, nint=4)
+    h = ctx.upload(loops)
+    try:
+        g, mean, sem = ctx.eval(h, fld, cx, cy, T, [1.0], group=128)
+        assert ctx.last_launches()[1] == "loop-parallel"
+    finally:
+        ctx.release(h)
+    ref = O.eval_groups(loops, cx, cy, T, [1.0], O.field("smooth", fermion=1, nint=4))
+    assert werr(g, ref) < W_TOL
+    assert np.all(sem >= 0)
+
+
+def test_same_alone_and_in_the_mix(ctx, wl):
+    """An instance's <W> does not depend on the batch it is evaluated in."""
+    loops = O.vloops(5, 256, 128)
+    cx, cy, T = _instances(300, 2.5, 0.02, 8.0, 3)
+    fld = wl.field("smooth", fermion=1, nint=4)
+    h = ctx.upload(loops)
+    try:
+        g_all, _, _ = ctx.eval(h, fld, cx, cy, T, [1.0, 2.0])
+        g_sub, _, _ = ctx.eval(h, fld, cx[:40], cy[:40], T[:40], [1.0, 2.0])
+        g_one, _, _ = ctx.eval(h, fld, cx[7:8], cy[7:8], T[7:8], [1.0, 2.0])
+    finally:
+        ctx.release(h)
+    assert werr(g_sub, g_all[:40]) < 1e-9
+    assert werr(g_one, g_all[7:8]) < W_TOL
+
+
+def test_legacy_EV_matches_reference_golden(wl, gold):
+    torch = pytest.importorskip("torch")
+    z, meta = gold
+    loops = z["loops"]
+    Nl, ppl = loops.shape[:2]
+    dev = torch.from_numpy(loops.reshape(-1)).cuda()
+    scal_d = torch.zeros(Nl * 4, device="cuda")
+    ferm_d = torch.zeros(Nl * 4, device="cuda")
+    scal_h = np.zeros((Nl, 4), dtype=np.float32)
+    ferm_h = np.zeros((Nl, 4), dtype=np.float32)
+    for case, ref in zip(meta["EV_CASES"], z["ev_out"]):
+        d, fe, l2, cx, T, F = case
+        wl.legacy_configure(d, nint=50)
+        p = wl.Wparams()
+        p.Nl, p.Nppl, p.F, p.l2, p.fermion, p.ng = Nl, ppl, F, l2, fe, Nl // 128
+        p.xcm.x, p.xcm.y = cx, 0.0
+        p.worldlines = dev.data_ptr()
+        p.Wsscal_d, p.Wsferm_d = scal_d.data_ptr(), ferm_d.data_ptr()
+        p.Wsscal_h = scal_h.ctypes.data
+        p.Wsferm_h = ferm_h.ctypes.data
+        got = np.array([wl.EV(T, p, np.arange(g * 128, (g + 1) * 128)) for g in range(Nl // 128)])
+        np.testing.assert_allclose(got, ref, rtol=W_TOL, err_msg=str(case))
+        # the reference's side effect: per-loop phases copied to Wsscal_h
+        s64, f64 = O.loops_phases(loops, cx, 0.0, T, F, O.field(d, fermion=fe, lambda2=l2))
+        assert np.abs(scal_h[:, :3] - s64).max() / np.abs(s64).max() < PHASE_TOL
+    wl.legacy_configure("smooth")
+
+
+def test_legacy_EV_rejects_host_pointers(wl):
+    p = wl.Wparams()
+    loops = np.zeros((128, 8, 4), dtype=np.float32)
+    p.Nl, p.Nppl, p.F, p.l2 = 128, 8, 1.0, 1.0
+    p.worldlines = loops.ctypes.data  # host memory: must be refused, not dereferenced
+    assert np.isnan(wl.EV(1.0, p, np.arange(128)))
+
+
+def test_invalid_arguments_return_status(ctx, wl):
+    loops = O.vloops(1, 128, 16)
+    h = ctx.upload(loops)
+    try:
+        with pytest.raises(wl.WlError) as e:
+            ctx.eval(h, wl.field("smooth", nint=3), [0.0], [0.0], [1.0], [1.0])
+        assert e.value.status == -1
+        with pytest.raises(wl.WlError):
+            ctx.eval(h, wl.field("smooth"), [0.0], [0.0], [-1.0], [1.0])
+        with pytest.raises(wl.WlError):
+            ctx.eval(h, wl.field("smooth"), [0.0], [0.0], [1.0], [1.0], group=100)
+        with pytest.raises(wl.WlError) as e:
+            ctx.eval(h + 1000, wl.field("smooth"), [0.0], [0.0], [1.0], [1.0])
+        assert e.value.status == -5
+        with pytest.raises(wl.WlError):
+            ctx.upload(np.zeros((4, 6, 4), dtype=np.float32))  # ppl not a multiple of 4
+    finally:
+        ctx.release(h)

@@ -1,0 +1,816 @@
+// wl_api.cpp -- C-ABI runtime of libwlgpu.so (include/wlgpu.h, wl_legacy.h).
+//
+// Owns contexts (device + stream + workspaces), resident loop ensembles, the
+// launch planning of the sweep kernels and the legacy EV() entry point of
+// intEV.cu:111-148.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/wl_legacy.h"
+#include "../../include/wlgpu.h"
+#include "wl_internal.h"
+
+using wl::FieldDev;
+
+namespace {
+
+// ------------------------------------------------------------ helpers --
+template <typename T>
+struct DevBuf {  // grow-only device buffer
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t want) {
+    if (want <= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc((void **)&p, want * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct Ensemble {
+  float4 *dev = nullptr;
+  int Nl = 0, ppl = 0;
+  bool owned = false;
+};
+
+typedef CUresult (*AddressRangeFn)(CUdeviceptr *, size_t *, CUdeviceptr);
+
+}  // namespace
+
+struct wl_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  std::map<int, Ensemble> ens;
+  int next_handle = 1;
+  DevBuf<float> inst;       // cx, cy, rtT, tq  (4 * ninst)
+  DevBuf<double> partial;   // sweep partial sums
+  DevBuf<double> out;       // group values, means, SEMs
+  DevBuf<int> status;       // device status word
+  DevBuf<int> list;         // EV() loop list
+  std::vector<float> h_inst;
+  std::string err;
+  int last_launches = 0;
+  const char *last_kind = "none";
+  AddressRangeFn addr_range = nullptr;
+};
+
+namespace {
+
+int fail(wl_ctx *ctx, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  return code;
+}
+
+int cuda_fail(wl_ctx *ctx, cudaError_t e, const char *what) {
+  return fail(ctx, WL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define WL_CHECK(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);  \
+  } while (0)
+
+// Device memory covering [p, p + bytes) on the context's device?  Refuses
+// host pointers before any kernel can dereference them.
+int check_device_range(wl_ctx *ctx, const void *p, size_t bytes, const char *name) {
+  if (!p) return fail(ctx, WL_ERR_INVALID, "%s is NULL", name);
+  if ((uintptr_t)p % 16 != 0) return fail(ctx, WL_ERR_INVALID, "%s is not 16-byte aligned", name);
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_INVALID, "%s is not a CUDA pointer", name);
+  }
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+    return fail(ctx, WL_ERR_INVALID, "%s is not device memory", name);
+  if (at.type == cudaMemoryTypeDevice && at.device != ctx->device)
+    return fail(ctx, WL_ERR_INVALID, "%s lives on device %d, context on %d", name, at.device,
+                ctx->device);
+  if (ctx->addr_range) {
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    if (ctx->addr_range(&base, &size, (CUdeviceptr)(uintptr_t)p) == CUDA_SUCCESS) {
+      if ((uintptr_t)p + bytes > (uintptr_t)base + size)
+        return fail(ctx, WL_ERR_INVALID, "%s: %zu bytes exceed its allocation", name, bytes);
+    }
+  }
+  return WL_OK;
+}
+
+int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
+  if (!f) return fail(ctx, WL_ERR_INVALID, "field is NULL");
+  int p = f->profile;
+  if (!(p == WL_PROFILE_STEP || p == WL_PROFILE_SMOOTH || p == WL_PROFILE_QUADRATIC ||
+        p == WL_PROFILE_GAUSSIAN || p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX))
+    return fail(ctx, WL_ERR_INVALID, "unsupported profile %d", p);
+  if (f->nint < 2 || f->nint > 64 || f->nint % 2)
+    return fail(ctx, WL_ERR_INVALID, "nint must be even in [2, 64], got %d", f->nint);
+  if (f->mode != WL_MODE_REFCOMPAT && f->mode != WL_MODE_EXACT)
+    return fail(ctx, WL_ERR_INVALID, "unknown mode %d", f->mode);
+  if (!(f->lambda2 > 0.0) || !isfinite(f->lambda2))
+    return fail(ctx, WL_ERR_INVALID, "lambda2 must be positive");
+  if ((p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX) &&
+      (!(f->tubedist > 0.0) || !isfinite(f->tubedist)))
+    return fail(ctx, WL_ERR_INVALID, "tubedist must be positive");
+  if (p == WL_PROFILE_FIXFLUX && !(f->tubedist > f->lmin))
+    return fail(ctx, WL_ERR_INVALID, "fixflux needs tubedist > lmin");
+  *kprofile = (p == WL_PROFILE_FIXFLUX && f->ff_variant) ? wl::kFixfluxFF : p;
+  memset(d, 0, sizeof(*d));
+  d->l2 = (float)f->lambda2;
+  d->inv_l2 = 1.0f / d->l2;
+  d->lam = sqrtf(d->l2);
+  d->a = (float)f->tubedist;
+  d->lmin = (float)f->lmin;
+  if (p == WL_PROFILE_FIXFLUX) {
+    d->lml = (d->lam - d->lmin) / (d->a - d->lmin);
+    d->aml = (d->a - d->lam) / (d->a - d->lmin);
+  }
+  d->nint = f->nint;
+  d->h = 1.0f / (float)f->nint;
+  if (f->mode == WL_MODE_REFCOMPAT) {
+    d->clampA = d->clampB = d->clampC = d->clampE = 1.0e-8f;
+    d->clampI = 1.0e-10f;
+  } else {
+    const bool divides = (p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX);
+    const float fl = divides ? 1.0e-30f : -INFINITY;
+    d->clampA = d->clampE = d->clampI = fl;
+    d->clampB = d->clampC = -INFINITY;
+  }
+  return WL_OK;
+}
+
+int lookup(wl_ctx *ctx, int handle, Ensemble *e) {
+  auto it = ctx->ens.find(handle);
+  if (it == ctx->ens.end()) return fail(ctx, WL_ERR_NOTFOUND, "unknown ensemble %d", handle);
+  *e = it->second;
+  return WL_OK;
+}
+
+int set_device(wl_ctx *ctx) {
+  WL_CHECK(ctx, cudaSetDevice(ctx->device));
+  return WL_OK;
+}
+
+// stage per-instance constants: cx, cy, rtT = float(sqrt(T)) (intEV.cu:118,
+// 124), tq = 4T/ppl (the 2T/(N/2) spin normalisation, intEV.cu:558-560)
+int upload_instances(wl_ctx *ctx, int ninst, const double *cx, const double *cy,
+                     const double *T, int ppl) {
+  for (int i = 0; i < ninst; ++i) {
+    if (!isfinite(cx[i]) || !isfinite(cy[i]) || !(T[i] > 0.0) || !isfinite(T[i]))
+      return fail(ctx, WL_ERR_INVALID, "instance %d: need finite centre and T > 0", i);
+  }
+  ctx->h_inst.resize((size_t)4 * ninst);
+  float *h = ctx->h_inst.data();
+  for (int i = 0; i < ninst; ++i) {
+    h[i] = (float)cx[i];
+    h[ninst + i] = (float)cy[i];
+    h[2 * ninst + i] = (float)sqrt(T[i]);
+    h[3 * ninst + i] = (float)(4.0 * T[i] / (double)ppl);
+  }
+  WL_CHECK(ctx, ctx->inst.reserve((size_t)4 * ninst));
+  WL_CHECK(ctx, cudaMemcpyAsync(ctx->inst.p, h, sizeof(float) * 4 * ninst,
+                                cudaMemcpyHostToDevice, ctx->stream));
+  return WL_OK;
+}
+
+// loops per CTA of the instance-parallel sweep: a divisor of the group size,
+// halved until the grid has at least ~12 CTAs per SM (load balance)
+int plan_chunk(wl_ctx *ctx, int ninst, int Nl, int group) {
+  const long tiles = (ninst + wl::kSweepThreads - 1) / wl::kSweepThreads;
+  int lc = group;
+  while (lc % 2 == 0 && lc > 1 && tiles * (long)(Nl / lc) < 12L * ctx->num_sms) lc /= 2;
+  return lc;
+}
+
+int check_status(wl_ctx *ctx) {
+  int st = 0;
+  WL_CHECK(ctx, cudaMemcpyAsync(&st, ctx->status.p, sizeof(int), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (st == wl::kDevTimeout)
+    return fail(ctx, WL_ERR_TIMEOUT, "a shared-memory stage copy timed out on the device");
+  if (st == wl::kDevBadInstance)
+    return fail(ctx, WL_ERR_INVALID, "an instance has T <= 0 or a non-finite value");
+  return WL_OK;
+}
+
+}  // namespace
+
+namespace {
+struct LegacyState {
+  std::mutex mu;
+  wl_field field = {WL_PROFILE_SMOOTH, 0, 50, WL_MODE_REFCOMPAT, 0, 0, 1.0, 1.0, 0.1};
+  int config_gen = 1;
+  wl_ctx *ctx = nullptr;
+  // cache key
+  bool valid = false;
+  double T = 0, F = 0, l2 = 0;
+  float cx = 0, cy = 0;
+  const void *loops = nullptr;
+  int Nl = 0, ppl = 0, fermion = 0, gen = 0;
+  DevBuf<double> w;    // per-loop W factors [Nl][3]
+  DevBuf<double> res;  // list mean
+};
+LegacyState &legacy() {
+  static LegacyState s;
+  return s;
+}
+}  // namespace
+
+// ================================================================ C ABI ==
+// Only the C entry points are exported (the build hides everything else).
+#pragma GCC visibility push(default)
+extern "C" {
+
+const char *wl_version(void) { return "wlgpu 0.1 (sm_103a)"; }
+
+const char *wl_status_string(int s) {
+  switch (s) {
+    case WL_OK: return "ok";
+    case WL_ERR_INVALID: return "invalid argument";
+    case WL_ERR_CUDA: return "CUDA error";
+    case WL_ERR_NOMEM: return "out of memory";
+    case WL_ERR_TIMEOUT: return "device wait timed out";
+    case WL_ERR_NOTFOUND: return "unknown handle";
+    case WL_ERR_ADMISSION: return "admission rejected";
+    default: return "unknown status";
+  }
+}
+
+int wl_ctx_create(int device, wl_ctx **out) {
+  if (!out) return WL_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return WL_ERR_CUDA;
+  }
+  wl_ctx *ctx = new wl_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) !=
+          cudaSuccess ||
+      ctx->status.reserve(1) != cudaSuccess ||
+      cudaMemset(ctx->status.p, 0, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return WL_ERR_CUDA;
+  }
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &fn, 12000, cudaEnableDefault,
+                                       &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    ctx->addr_range = (AddressRangeFn)fn;
+  cudaGetLastError();
+  *out = ctx;
+  return WL_OK;
+}
+
+int wl_ctx_destroy(wl_ctx *ctx) {
+  if (!ctx) return WL_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->ens)
+    if (kv.second.owned) cudaFree(kv.second.dev);
+  ctx->inst.release();
+  ctx->partial.release();
+  ctx->out.release();
+  ctx->status.release();
+  ctx->list.release();
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return WL_OK;
+}
+
+int wl_last_error(wl_ctx *ctx, char *buf, int buflen) {
+  if (!ctx || !buf || buflen <= 0) return WL_ERR_INVALID;
+  snprintf(buf, (size_t)buflen, "%s", ctx->err.c_str());
+  return WL_OK;
+}
+
+int wl_ctx_synchronize(wl_ctx *ctx) {
+  if (!ctx) return WL_ERR_INVALID;
+  int r = set_device(ctx);
+  if (r) return r;
+  r = check_status(ctx);
+  if (r != WL_OK) cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream);
+  return r;
+}
+
+static int check_shape(wl_ctx *ctx, int Nl, int ppl) {
+  if (Nl < 1 || ppl < 4 || ppl % 4 != 0)
+    return fail(ctx, WL_ERR_INVALID, "need Nl >= 1 and ppl a positive multiple of 4 (Nl=%d ppl=%d)",
+                Nl, ppl);
+  if ((double)Nl * (double)ppl > 2147483647.0)
+    return fail(ctx, WL_ERR_INVALID, "ensemble too large (%d x %d points)", Nl, ppl);
+  return WL_OK;
+}
+
+int wl_ensemble_upload(wl_ctx *ctx, const float *host_loops, int Nl, int ppl, int *handle) {
+  if (!ctx || !host_loops || !handle) return fail(ctx, WL_ERR_INVALID, "NULL argument");
+  int r = check_shape(ctx, Nl, ppl);
+  if (r) return r;
+  if ((r = set_device(ctx))) return r;
+  Ensemble e;
+  e.Nl = Nl;
+  e.ppl = ppl;
+  e.owned = true;
+  const size_t bytes = (size_t)Nl * ppl * sizeof(float4);
+  if (cudaMalloc((void **)&e.dev, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu bytes for the ensemble", bytes);
+  }
+  cudaError_t ce = cudaMemcpyAsync(e.dev, host_loops, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  if (ce != cudaSuccess) {
+    cudaFree(e.dev);
+    return cuda_fail(ctx, ce, "ensemble upload");
+  }
+  *handle = ctx->next_handle++;
+  ctx->ens[*handle] = e;
+  return WL_OK;
+}
+
+int wl_ensemble_wrap(wl_ctx *ctx, const float *dev_loops, int Nl, int ppl, int *handle) {
+  if (!ctx || !handle) return fail(ctx, WL_ERR_INVALID, "NULL argument");
+  int r = check_shape(ctx, Nl, ppl);
+  if (r) return r;
+  if ((r = set_device(ctx))) return r;
+  if ((r = check_device_range(ctx, dev_loops, (size_t)Nl * ppl * sizeof(float4), "dev_loops")))
+    return r;
+  Ensemble e;
+  e.dev = (float4 *)dev_loops;
+  e.Nl = Nl;
+  e.ppl = ppl;
+  e.owned = false;
+  *handle = ctx->next_handle++;
+  ctx->ens[*handle] = e;
+  return WL_OK;
+}
+
+int wl_ensemble_generate(wl_ctx *ctx, uint64_t seed, int first, int Nl, int ppl,
+                         int *handle) {
+  if (!ctx || !handle) return fail(ctx, WL_ERR_INVALID, "NULL argument");
+  int r = check_shape(ctx, Nl, ppl);
+  if (r) return r;
+  if (first < 0) return fail(ctx, WL_ERR_INVALID, "first must be >= 0");
+  if ((r = set_device(ctx))) return r;
+  Ensemble e;
+  e.Nl = Nl;
+  e.ppl = ppl;
+  e.owned = true;
+  const size_t bytes = (size_t)Nl * ppl * sizeof(float4);
+  if (cudaMalloc((void **)&e.dev, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu bytes for the ensemble", bytes);
+  }
+  cudaError_t ce = wl::launch_vloops(seed, first, Nl, ppl, e.dev, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  if (ce != cudaSuccess) {
+    cudaFree(e.dev);
+    return cuda_fail(ctx, ce, "loop generator");
+  }
+  *handle = ctx->next_handle++;
+  ctx->ens[*handle] = e;
+  return WL_OK;
+}
+
+int wl_ensemble_download(wl_ctx *ctx, int handle, float *host_loops) {
+  if (!ctx || !host_loops) return fail(ctx, WL_ERR_INVALID, "NULL argument");
+  Ensemble e;
+  int r = lookup(ctx, handle, &e);
+  if (r) return r;
+  if ((r = set_device(ctx))) return r;
+  WL_CHECK(ctx, cudaMemcpyAsync(host_loops, e.dev, (size_t)e.Nl * e.ppl * sizeof(float4),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+  return WL_OK;
+}
+
+int wl_ensemble_release(wl_ctx *ctx, int handle) {
+  if (!ctx) return WL_ERR_INVALID;
+  Ensemble e;
+  int r = lookup(ctx, handle, &e);
+  if (r) return r;
+  if ((r = set_device(ctx))) return r;
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (e.owned) cudaFree(e.dev);
+  ctx->ens.erase(handle);
+  return WL_OK;
+}
+
+int wl_ensemble_info(wl_ctx *ctx, int handle, const float **dev_loops, int *Nl, int *ppl) {
+  if (!ctx) return WL_ERR_INVALID;
+  Ensemble e;
+  int r = lookup(ctx, handle, &e);
+  if (r) return r;
+  if (dev_loops) *dev_loops = (const float *)e.dev;
+  if (Nl) *Nl = e.Nl;
+  if (ppl) *ppl = e.ppl;
+  return WL_OK;
+}
+
+// Validation shared by the two eval entry points.
+static int eval_prologue(wl_ctx *ctx, int handle, const wl_field *field, int ninst, int nF,
+                         const double *host_F, int group, Ensemble *e, int *kprof,
+                         FieldDev *fd) {
+  if (!host_F) return fail(ctx, WL_ERR_INVALID, "NULL flux array");
+  if (ninst < 1) return fail(ctx, WL_ERR_INVALID, "ninst must be >= 1");
+  if (nF < 1 || nF > wl::kMaxF) return fail(ctx, WL_ERR_INVALID, "nF must be in [1, %d]", wl::kMaxF);
+  int r = lookup(ctx, handle, e);
+  if (r) return r;
+  if (group < 1 || e->Nl % group != 0)
+    return fail(ctx, WL_ERR_INVALID, "group %d must divide Nl = %d", group, e->Nl);
+  if ((r = field_to_dev(ctx, field, kprof, fd))) return r;
+  for (int j = 0; j < nF; ++j)
+    if (!isfinite(host_F[j])) return fail(ctx, WL_ERR_INVALID, "F[%d] is not finite", j);
+  return set_device(ctx);
+}
+
+// Sweep + reduction on the context stream; instances are already staged in
+// ctx->inst as [cx | cy | rtT | tq].  Outputs are device pointers (may be
+// NULL).  Returns after enqueueing.
+static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &fd,
+                    bool fermion, int nint, int ninst, int nF, const double *host_F, int group,
+                    double *dg, double *dm, double *ds) {
+  const bool use_sweep = ninst >= 32;
+  int n_chunks, cpg;
+  if (use_sweep) {
+    const int lc = plan_chunk(ctx, ninst, e.Nl, group);
+    n_chunks = e.Nl / lc;
+    cpg = group / lc;
+  } else {
+    n_chunks = e.Nl;
+    cpg = group;
+  }
+  const size_t npart = (size_t)n_chunks * nF * 3 * ninst;
+  if (ctx->partial.reserve(npart) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu partial sums", npart);
+  }
+  const float *di = ctx->inst.p;
+  if (use_sweep) {
+    wl::SweepArgs a;
+    memset(&a, 0, sizeof(a));
+    a.loops = e.dev;
+    a.Nl = e.Nl;
+    a.ppl = e.ppl;
+    a.ninst = ninst;
+    a.cx = di;
+    a.cy = di + ninst;
+    a.rtT = di + 2 * ninst;
+    a.tq = di + 3 * ninst;
+    a.nF = nF;
+    for (int j = 0; j < nF; ++j) a.F[j] = (float)host_F[j];
+    a.field = fd;
+    a.chunk_loops = e.Nl / n_chunks;
+    a.n_chunks = n_chunks;
+    a.partial = ctx->partial.p;
+    a.status = ctx->status.p;
+    a.wait_tries = 1u << 22;
+    WL_CHECK(ctx, wl::launch_sweep(kprof, fermion, nint, a, ctx->stream));
+    ctx->last_kind = "instance-parallel";
+  } else {
+    wl::LoopArgs a;
+    memset(&a, 0, sizeof(a));
+    a.loops = e.dev;
+    a.Nl = e.Nl;
+    a.ppl = e.ppl;
+    a.ninst = ninst;
+    a.cx = di;
+    a.cy = di + ninst;
+    a.rtT = di + 2 * ninst;
+    a.tq = di + 3 * ninst;
+    a.nF = nF;
+    for (int j = 0; j < nF; ++j) a.F[j] = (float)host_F[j];
+    a.field = fd;
+    a.partial = ctx->partial.p;
+    WL_CHECK(ctx, wl::launch_loopwarp(kprof, fermion, nint, a, ctx->stream));
+    ctx->last_kind = "loop-parallel";
+  }
+  WL_CHECK(ctx, wl::launch_group_reduce(ctx->partial.p, n_chunks, cpg, group, ninst, nF, dg, dm,
+                                        ds, ctx->stream));
+  return WL_OK;
+}
+
+int wl_eval(wl_ctx *ctx, int handle, const wl_field *field, int ninst, const double *host_cx,
+            const double *host_cy, const double *host_T, int nF, const double *host_F,
+            int group, double *out_group, double *out_mean, double *out_sem) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (!host_cx || !host_cy || !host_T) return fail(ctx, WL_ERR_INVALID, "NULL instance arrays");
+  Ensemble e;
+  int kprof;
+  FieldDev fd;
+  int r = eval_prologue(ctx, handle, field, ninst, nF, host_F, group, &e, &kprof, &fd);
+  if (r) return r;
+  if ((r = upload_instances(ctx, ninst, host_cx, host_cy, host_T, e.ppl))) return r;
+  WL_CHECK(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+  const int ng = e.Nl / group;
+  const size_t nout = (size_t)ninst * nF * (ng + 2);
+  if (ctx->out.reserve(nout) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu outputs", nout);
+  }
+  double *dg = ctx->out.p, *dm = dg + (size_t)ninst * nF * ng, *ds = dm + (size_t)ninst * nF;
+  if ((r = run_eval(ctx, e, kprof, fd, field->fermion != 0, field->nint, ninst, nF, host_F,
+                    group, dg, dm, ds)))
+    return r;
+  ctx->last_launches = 2;
+  if (out_group)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_group, dg, sizeof(double) * ninst * nF * ng,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  if (out_mean)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_mean, dm, sizeof(double) * ninst * nF,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  if (out_sem)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_sem, ds, sizeof(double) * ninst * nF,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  return check_status(ctx);
+}
+
+int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
+                   const double *dev_cx, const double *dev_cy, const double *dev_T, int nF,
+                   const double *host_F, int group, double *dev_out_group, double *dev_out_mean,
+                   double *dev_out_sem) {
+  if (!ctx) return WL_ERR_INVALID;
+  Ensemble e;
+  int kprof;
+  FieldDev fd;
+  int r = eval_prologue(ctx, handle, field, ninst, nF, host_F, group, &e, &kprof, &fd);
+  if (r) return r;
+  const size_t nb = (size_t)ninst * sizeof(double);
+  if ((r = check_device_range(ctx, dev_cx, nb, "dev_cx")) ||
+      (r = check_device_range(ctx, dev_cy, nb, "dev_cy")) ||
+      (r = check_device_range(ctx, dev_T, nb, "dev_T")))
+    return r;
+  const int ng = e.Nl / group;
+  if (dev_out_group &&
+      (r = check_device_range(ctx, dev_out_group, nb * nF * ng, "dev_out_group")))
+    return r;
+  if (dev_out_mean && (r = check_device_range(ctx, dev_out_mean, nb * nF, "dev_out_mean")))
+    return r;
+  if (dev_out_sem && (r = check_device_range(ctx, dev_out_sem, nb * nF, "dev_out_sem")))
+    return r;
+  WL_CHECK(ctx, ctx->inst.reserve((size_t)4 * ninst));
+  WL_CHECK(ctx, wl::launch_instance_setup(dev_cx, dev_cy, dev_T, ninst, e.ppl, ctx->inst.p,
+                                          ctx->status.p, ctx->stream));
+  if ((r = run_eval(ctx, e, kprof, fd, field->fermion != 0, field->nint, ninst, nF, host_F,
+                    group, dev_out_group, dev_out_mean, dev_out_sem)))
+    return r;
+  ctx->last_launches = 3;
+  return WL_OK;
+}
+
+int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s) {
+  if (!ctx || !ops_per_s || (kind != 0 && kind != 1)) return fail(ctx, WL_ERR_INVALID, "bad probe");
+  int r = set_device(ctx);
+  if (r) return r;
+  const int threads = 256, blocks = ctx->num_sms * 8;
+  const int iters = kind == 0 ? 4096 : 1024;
+  if (ctx->partial.reserve((size_t)blocks) != cudaSuccess) return fail(ctx, WL_ERR_NOMEM, "probe");
+  float *sink = (float *)ctx->partial.p;
+  cudaEvent_t e0, e1;
+  WL_CHECK(ctx, cudaEventCreate(&e0));
+  WL_CHECK(ctx, cudaEventCreate(&e1));
+  WL_CHECK(ctx, wl::launch_peak_probe(kind, blocks, threads, iters, sink, ctx->stream));  // warm
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    WL_CHECK(ctx, cudaEventRecord(e0, ctx->stream));
+    WL_CHECK(ctx, wl::launch_peak_probe(kind, blocks, threads, iters, sink, ctx->stream));
+    WL_CHECK(ctx, cudaEventRecord(e1, ctx->stream));
+    WL_CHECK(ctx, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    WL_CHECK(ctx, cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ops_per_s = (double)blocks * threads * iters * 8.0 / (best * 1e-3);
+  return WL_OK;
+}
+
+int wl_ctx_stream(wl_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return WL_ERR_INVALID;
+  *stream = (void *)ctx->stream;
+  return WL_OK;
+}
+
+int wl_loops(wl_ctx *ctx, int handle, const wl_field *field, double cx, double cy, double T,
+             double F, float *host_scal, float *host_ferm) {
+  if (!ctx) return WL_ERR_INVALID;
+  Ensemble e;
+  int r = lookup(ctx, handle, &e);
+  if (r) return r;
+  int kprof;
+  FieldDev fd;
+  if ((r = field_to_dev(ctx, field, &kprof, &fd))) return r;
+  if (!isfinite(F)) return fail(ctx, WL_ERR_INVALID, "F is not finite");
+  if ((r = set_device(ctx))) return r;
+  if ((r = upload_instances(ctx, 1, &cx, &cy, &T, e.ppl))) return r;
+  if (ctx->partial.reserve((size_t)e.Nl * 3 + (size_t)e.Nl * 8) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate per-loop outputs");
+  }
+  // partial: [Nl][3] doubles, then two float4 [Nl] arrays (16-byte aligned)
+  float4 *ds = (float4 *)(ctx->partial.p + (((size_t)e.Nl * 3 + 1) & ~(size_t)1));
+  float4 *df = ds + e.Nl;
+  WL_CHECK(ctx, cudaMemsetAsync(df, 0, sizeof(float4) * e.Nl, ctx->stream));
+  wl::LoopArgs a;
+  memset(&a, 0, sizeof(a));
+  a.loops = e.dev;
+  a.Nl = e.Nl;
+  a.ppl = e.ppl;
+  a.ninst = 1;
+  a.cx = ctx->inst.p;
+  a.cy = ctx->inst.p + 1;
+  a.rtT = ctx->inst.p + 2;
+  a.tq = ctx->inst.p + 3;
+  a.nF = 1;
+  a.F[0] = (float)F;
+  a.field = fd;
+  a.partial = ctx->partial.p;
+  a.scal = ds;
+  a.ferm = df;
+  WL_CHECK(ctx, wl::launch_loopwarp(kprof, field->fermion != 0, field->nint, a, ctx->stream));
+  ctx->last_launches = 1;
+  ctx->last_kind = "loop-parallel";
+  if (host_scal)
+    WL_CHECK(ctx, cudaMemcpyAsync(host_scal, ds, sizeof(float4) * e.Nl, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  if (host_ferm)
+    WL_CHECK(ctx, cudaMemcpyAsync(host_ferm, df, sizeof(float4) * e.Nl, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+  return WL_OK;
+}
+
+int wl_last_launches(wl_ctx *ctx, int *launches, const char **kind) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (launches) *launches = ctx->last_launches;
+  if (kind) *kind = ctx->last_kind;
+  return WL_OK;
+}
+
+// ================================================================ legacy ==
+// EV() keeps the reference's signature and side effects (intEV.cu:111-148):
+// it computes every loop of the ensemble at (T, xcm), writes the per-loop
+// phases into the caller's Wsscal_d / Wsferm_d and copies them to
+// Wsscal_h / Wsferm_h, then returns the Richardson-combined mean over the
+// 128 loops of WLlist.  The per-loop W factors of the last (T, xcm, field)
+// stay cached on the device, so the ng calls of one Tfunc() evaluation
+// (Integrand.c:249-305) cost one sweep and ng list reductions.
+int wl_legacy_configure(int profile, double tubedist, double lmin, int nint, int mode) {
+  LegacyState &L = legacy();
+  std::lock_guard<std::mutex> lk(L.mu);
+  wl_field f = L.field;
+  f.profile = profile;
+  f.tubedist = tubedist;
+  f.lmin = lmin;
+  f.nint = nint;
+  f.mode = mode;
+  f.lambda2 = 1.0;
+  int kp;
+  FieldDev d;
+  int r = field_to_dev(nullptr, &f, &kp, &d);
+  if (r) return r;
+  L.field = f;
+  L.config_gen++;
+  L.valid = false;
+  return WL_OK;
+}
+
+int wl_legacy_query(int *profile, double *tubedist, double *lmin, int *nint, int *mode) {
+  LegacyState &L = legacy();
+  std::lock_guard<std::mutex> lk(L.mu);
+  if (profile) *profile = L.field.profile;
+  if (tubedist) *tubedist = L.field.tubedist;
+  if (lmin) *lmin = L.field.lmin;
+  if (nint) *nint = L.field.nint;
+  if (mode) *mode = L.field.mode;
+  return WL_OK;
+}
+
+static double legacy_fail(const char *msg) {
+  fprintf(stderr, "EV(): %s\n", msg);
+  return NAN;
+}
+
+double EV(double T, void *p, int *WLlist) {
+  if (!p || !WLlist) return legacy_fail("NULL argument");
+  const struct Wparams params = *(const struct Wparams *)p;
+  LegacyState &L = legacy();
+  std::lock_guard<std::mutex> lk(L.mu);
+  const int groupsize = 128;  // intEV.cu:117
+  if (!L.ctx) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    cudaGetLastError();
+    if (wl_ctx_create(dev, &L.ctx) != WL_OK) return legacy_fail("no CUDA device");
+  }
+  wl_ctx *ctx = L.ctx;
+  if (set_device(ctx)) return legacy_fail(ctx->err.c_str());
+  if (check_shape(ctx, params.Nl, params.Nppl)) return legacy_fail(ctx->err.c_str());
+  if (params.Nl < groupsize) return legacy_fail("Nl is smaller than one group of 128");
+  for (int j = 0; j < groupsize; ++j)
+    if (WLlist[j] < 0 || WLlist[j] >= params.Nl) return legacy_fail("WLlist index out of range");
+  wl_field f = L.field;
+  f.fermion = params.fermion == 1;
+  f.lambda2 = params.l2;
+  int kprof;
+  FieldDev fd;
+  if (field_to_dev(ctx, &f, &kprof, &fd)) return legacy_fail(ctx->err.c_str());
+  const bool hit = L.valid && L.T == T && L.F == params.F && L.l2 == params.l2 &&
+                   L.cx == params.xcm.x && L.cy == params.xcm.y &&
+                   L.loops == params.worldlines && L.Nl == params.Nl && L.ppl == params.Nppl &&
+                   L.fermion == f.fermion && L.gen == L.config_gen;
+  if (!hit) {
+    L.valid = false;
+    const size_t npts = (size_t)params.Nl * params.Nppl;
+    if (check_device_range(ctx, params.worldlines, npts * sizeof(float4), "worldlines") ||
+        check_device_range(ctx, params.Wsscal_d, params.Nl * sizeof(float4), "Wsscal_d") ||
+        (f.fermion &&
+         check_device_range(ctx, params.Wsferm_d, params.Nl * sizeof(float4), "Wsferm_d")))
+      return legacy_fail(ctx->err.c_str());
+    const double cx = params.xcm.x, cy = params.xcm.y;
+    if (upload_instances(ctx, 1, &cx, &cy, &T, params.Nppl)) return legacy_fail(ctx->err.c_str());
+    if (L.w.reserve((size_t)params.Nl * 3) != cudaSuccess) return legacy_fail("out of memory");
+    wl::LoopArgs a;
+    memset(&a, 0, sizeof(a));
+    a.loops = params.worldlines;
+    a.Nl = params.Nl;
+    a.ppl = params.Nppl;
+    a.ninst = 1;
+    a.cx = ctx->inst.p;
+    a.cy = ctx->inst.p + 1;
+    a.rtT = ctx->inst.p + 2;
+    a.tq = ctx->inst.p + 3;
+    a.nF = 1;
+    a.F[0] = (float)params.F;
+    a.field = fd;
+    a.partial = L.w.p;
+    a.scal = params.Wsscal_d;
+    a.ferm = f.fermion ? params.Wsferm_d : nullptr;
+    cudaError_t ce = wl::launch_loopwarp(kprof, f.fermion != 0, f.nint, a, ctx->stream);
+    if (ce == cudaSuccess && params.Wsscal_h)
+      ce = cudaMemcpyAsync(params.Wsscal_h, params.Wsscal_d, params.Nl * sizeof(float4),
+                           cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce == cudaSuccess && f.fermion && params.Wsferm_h)
+      ce = cudaMemcpyAsync(params.Wsferm_h, params.Wsferm_d, params.Nl * sizeof(float4),
+                           cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce != cudaSuccess) return legacy_fail(cudaGetErrorString(ce));
+    L.T = T;
+    L.F = params.F;
+    L.l2 = params.l2;
+    L.cx = params.xcm.x;
+    L.cy = params.xcm.y;
+    L.loops = params.worldlines;
+    L.Nl = params.Nl;
+    L.ppl = params.Nppl;
+    L.fermion = f.fermion;
+    L.gen = L.config_gen;
+    L.valid = true;
+  }
+  if (ctx->list.reserve(groupsize) != cudaSuccess || L.res.reserve(1) != cudaSuccess)
+    return legacy_fail("out of memory");
+  double ev = NAN;
+  cudaError_t ce = cudaMemcpyAsync(ctx->list.p, WLlist, sizeof(int) * groupsize,
+                                   cudaMemcpyHostToDevice, ctx->stream);
+  if (ce == cudaSuccess) ce = wl::launch_list_mean(L.w.p, ctx->list.p, groupsize, L.res.p, ctx->stream);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(&ev, L.res.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  if (ce != cudaSuccess) {
+    L.valid = false;
+    return legacy_fail(cudaGetErrorString(ce));
+  }
+  return ev;
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

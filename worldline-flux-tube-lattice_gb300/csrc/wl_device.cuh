@@ -1,0 +1,394 @@
+// wl_device.cuh -- device building blocks of the Wilson-loop kernels (sm_103a).
+//
+// Field profiles, the Simpson segment integral, the per-loop W factors and
+// the bulk-copy / mbarrier primitives used to stage loops in shared memory.
+// Reference semantics are cited per function (intEV.cu, intEVff.cu,
+// Integrand.c line numbers).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "wl_types.h"
+
+namespace wl {
+
+// ---------------------------------------------------------------- math --
+// Single-instruction MUFU operations, PTX-documented accuracy: rcp.approx
+// max 1 ulp; ex2.approx max relative error 2^-22 (ftz: no subnormals).
+__device__ __forceinline__ float rcp_fast(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float ex2_fast(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// e^-x for x >= 0 through 2^(-x log2 e)
+__device__ __forceinline__ float expneg_fast(float x) {
+  return ex2_fast(-1.4426950408889634f * x);
+}
+
+// (1 - e^-x) / x for 0 <= x < 0.5 from its Taylor series sum_k (-x)^k/(k+1)!
+// truncated after x^8 (remainder < x^9/10! < 6e-10).
+__device__ __forceinline__ float one_minus_expneg_over_x(float x) {
+  float p = 1.0f / 362880.0f;
+  p = fmaf(p, -x, 1.0f / 40320.0f);
+  p = fmaf(p, -x, 1.0f / 5040.0f);
+  p = fmaf(p, -x, 1.0f / 720.0f);
+  p = fmaf(p, -x, 1.0f / 120.0f);
+  p = fmaf(p, -x, 1.0f / 24.0f);
+  p = fmaf(p, -x, 1.0f / 6.0f);
+  p = fmaf(p, -x, 0.5f);
+  p = fmaf(p, -x, 1.0f);
+  return p;
+}
+
+// ------------------------------------------------------------- profiles --
+// Each profile returns, at rho^2 = r2:
+//   g  = f_lambda(r2) / r2        (scalar Simpson integrand, intEV.cu:425-449)
+//   fp = f'_lambda(r2) / FpScale  (spinor integrand, intEV.cu:430-451)
+// fp is scaled so that the per-node work is minimal; the constant factor is
+// applied once per loop (fp_scale()).
+
+// exponential integral Ei(x) = -E1(-x), x < -1, by Lentz's continued
+// fraction with the reference's stopping rule (intEV.cu:29-61)
+__device__ __forceinline__ float expint_lentz(float x) {
+  float b = -x + 1.0f, c = 1.0e10f, d = 1.0f / b, h = d;
+  for (int i = 1; i <= 400; i++) {
+    float an = -(float)i * (float)i;
+    b += 2.0f;
+    d = 1.0f / (an * d + b);
+    c = b + an / c;
+    float del = c * d;
+    h *= del;
+    if (fabsf(del - 1.0f) <= 1.0e-6f) return -h * expf(x);
+  }
+  return 0.0f;
+}
+
+__device__ __forceinline__ float bump_d(float x) {  // intEV.cu:151-159
+  return (x * x < 0.999f) ? expf(-1.0f / (1.0f - x * x)) : 0.0f;
+}
+
+template <bool FF>
+__device__ __forceinline__ float phi_d(float x) {  // intEV.cu:161-174 / intEVff.cu:147-157
+  const float onemx2 = 1.0f - x * x;
+  if (x < (FF ? 1.0f : 0.999f))
+    return 1.0f - (0.5f / 0.0742478f) *
+                      (onemx2 * expf(-1.0f / onemx2) + expint_lentz(-1.0f / onemx2));
+  return 1.0f;
+}
+
+template <bool FF>
+__device__ __forceinline__ float chi_d(float x, float n, float lam, float a) {
+  // intEV.cu:176-198 (logistic fit) / intEVff.cu:159-176 (cosh-ratio fit)
+  const float onemx2 = 1.0f - x * x, x2 = x * x, x4 = x2 * x2;
+  if (x <= (FF ? -1.0f : -0.999f)) return 0.0f;
+  if (x2 < (FF ? 1.0f : 0.999f)) {
+    float ans = 0.5f * (-onemx2 * expf(-1.0f / onemx2) - expint_lentz(-1.0f / onemx2));
+    if (FF)
+      ans += 2.0f * n * a / lam *
+             (0.218f + 0.393f * x * coshf(0.806f * x4 - 0.696f * x2 + 0.0902f) /
+                           coshf(0.825f * x2 - 0.0234f * x + 0.375f));
+    else
+      ans += 2.0f * n * a / lam * 0.444f /
+             (1.0f + expf(-(3.31f * x + 5.25f * x * x2 * sinf(x) *
+                                            cosf(-0.907f * x2 - 1.29f * x4 * x4)) /
+                          cosf(x)));
+    return ans;
+  }
+  return 2.0f * n * a * 0.443991f / lam;
+}
+
+template <int P>
+struct Profile;
+
+template <>
+struct Profile<kSmooth> {  // f = r2/(l2+r2): f/r2 = 1/(l2+r2), f' = l2 (f/r2)^2
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    g = rcp_fast(F.l2 + r2);
+    fp = g * g;
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &F) { return F.l2; }
+  static constexpr bool kHeavy = false;
+};
+
+template <>
+struct Profile<kStep> {  // intEV.cu:267-272, 368-373
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    const bool in = r2 < F.l2;
+    g = in ? F.inv_l2 : rcp_fast(r2);
+    fp = in ? 1.0f : 0.0f;
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &F) { return F.inv_l2; }
+  static constexpr bool kHeavy = false;
+};
+
+template <>
+struct Profile<kQuadratic> {  // intEV.cu:276-281, 377-382
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    const bool in = r2 < F.l2;
+    const float u = r2 * F.inv_l2;
+    g = in ? (2.0f - u) * F.inv_l2 : rcp_fast(r2);
+    fp = in ? 1.0f - u : 0.0f;
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &F) {
+    return 2.0f * F.inv_l2;
+  }
+  static constexpr bool kHeavy = false;
+};
+
+template <>
+struct Profile<kGaussian> {  // f = 1 - e^{-r2/l2} (intEV.cu:282-284, 383-385)
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    const float x = r2 * F.inv_l2;
+    const float e = expneg_fast(x);
+    // below x = 0.5 the series avoids the cancellation of 1 - e^-x
+    g = (x < 0.5f) ? one_minus_expneg_over_x(x) * F.inv_l2 : (1.0f - e) * rcp_fast(r2);
+    fp = e;
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &F) { return F.inv_l2; }
+  static constexpr bool kHeavy = false;
+};
+
+// The lattice profiles below are heavy (loops, several transcendentals per
+// node): they are compiled only with a run-time interval count and without
+// unrolling, which keeps code size and build time bounded.
+template <>
+struct Profile<kPeriodic> {  // radial shells, intEV.cu:201-232 and 300-328
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    const float rho = sqrtf(r2), a = F.a, lam = F.lam;
+    const float flraf = floorf(rho / a);
+    const int i0 = (int)flraf - 2, i1 = (int)flraf + 2;
+    float f = (i0 > 0) ? 0.5f * (flraf - 3.0f) * (flraf - 2.0f) : 0.0f;
+    float d = 0.0f;
+    for (int i = i0; i <= i1; i++) {
+      if (i == 0) {
+        const float ex = expf(-rho / lam), ex1 = 1.0f + ex;
+        f = -rho / a * (ex / ex1) - lam / a * logf(ex1);
+        d = ex / (a * ex1 * ex1);
+      } else if (i > 0) {
+        const float ea = expf(-(rho - (float)i * a) / lam), ea1 = 1.0f + ea;
+        f = f + (float)i / ea1;
+        d = d + ((float)i / rho) * ea / (ea1 * ea1);
+      }
+    }
+    const float ln2 = 0.69314718055994531f;
+    g = (a / (lam * ln2) * f + 1.0f) / r2;
+    fp = a / (2.0f * F.l2 * ln2) * d;
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &) { return 1.0f; }
+  static constexpr bool kHeavy = true;
+};
+
+template <bool FF>
+struct FixfluxProfile {  // intEV.cu:236-257, 333-357; intEVff.cu:194-250
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    const float a = F.a, lam = F.lam, lml = F.lml, aml = F.aml;
+    const float rho = sqrtf(r2);
+    const float n = floorf((rho + 0.5f * a) / a);
+    float f;
+    if (r2 <= 0.25f * a * a) {
+      f = (1.0f - 0.75f * lml) * phi_d<FF>(2.0f * sqrtf(r2 * F.inv_l2)) +
+          3.0f * r2 / (a * a) * lml;
+    } else {
+      f = 1.0f + 0.75f * (4.0f * r2 / (a * a) - 1.0f) * lml + 3.0f * n * (n - 1.0f) * aml;
+      f += 3.0f * lam / (0.443991f * a) * aml *
+           chi_d<FF>(2.0f * (rho - n * a) / lam, n, lam, a);
+    }
+    g = f / r2;
+    const float bbg = 3.0f / (a * a) * lml;
+    if (rho <= 0.5f * a)
+      fp = bbg + 2.0f / (F.l2 * 0.0742478f) * (1.0f - 0.75f * lml) * bump_d(2.0f * rho / lam);
+    else
+      fp = bbg + 6.0f / (0.443991f * lam * a) * aml * bump_d(2.0f * (rho - n * a) / lam);
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &) { return 1.0f; }
+  static constexpr bool kHeavy = true;
+};
+template <>
+struct Profile<kFixflux> : FixfluxProfile<false> {};
+template <>
+struct Profile<kFixfluxFF> : FixfluxProfile<true> {};
+
+// ------------------------------------------------------------- segment --
+// One segment z_i -> z_j of a sub-loop (intEV.cu:526-552 with Idt,
+// intEV.cu:408-459): rho^2(t) = a + 2bt + ct^2 with a = |z_i|^2,
+// b = z_i.(z_j - z_i), c = |z_j - z_i|^2, composite Simpson with NINT
+// intervals.  Adds xyyx * sum_w(f/rho^2) to ph and sum_w(f') to sp; the
+// Simpson factor h/3 and the f' scale are applied once per loop.
+template <int P, bool FERM, int NINT>
+__device__ __forceinline__ void segment(float zix, float ziy, float zjx, float zjy,
+                                        const FieldDev &F, float &ph, float &sp) {
+  static_assert(NINT == 0 || (NINT % 2 == 0 && NINT >= 2), "Simpson needs an even interval count");
+  const float dx = zjx - zix, dy = zjy - ziy;
+  float a = fmaf(zix, zix, ziy * ziy);
+  float b = fmaf(zix, dx, ziy * dy);
+  float c = fmaf(dx, dx, dy * dy);
+  const float xyyx = fmaf(zix, zjy, -(ziy * zjx));
+  a = fmaxf(a, F.clampA);
+  b = fmaxf(b, F.clampB);
+  c = fmaxf(c, F.clampC);
+  const float b2 = b + b;
+  const float ae = fmaxf(a + b2 + c, F.clampE);
+  float g0, f0, g1, f1;
+  Profile<P>::eval(a, F, g0, f0);
+  Profile<P>::eval(ae, F, g1, f1);
+  float so = 0.0f, se = 0.0f, fo = 0.0f, fe = 0.0f;
+  auto node = [&](int j, float t) {
+    const float r2 = fmaxf(fmaf(fmaf(c, t, b2), t, a), F.clampI);
+    float g, fp;
+    Profile<P>::eval(r2, F, g, fp);
+    if (j & 1) {
+      so += g;
+      if (FERM) fo += fp;
+    } else {
+      se += g;
+      if (FERM) fe += fp;
+    }
+  };
+  if constexpr (NINT > 0) {
+#pragma unroll
+    for (int j = 1; j < NINT; j++)
+      // the reference's abscissa (float)j * h with h = 1.0f/n (intEV.cu:416, 436)
+      node(j, (float)j * (1.0f / (float)NINT));
+  } else {
+#pragma unroll 1
+    for (int j = 1; j < F.nint; j++) node(j, (float)j * F.h);
+  }
+  const float S = fmaf(4.0f, so, fmaf(2.0f, se, g0 + g1));
+  ph = fmaf(xyyx, S, ph);
+  if (FERM) sp += fmaf(4.0f, fo, fmaf(2.0f, fe, f0 + f1));
+}
+
+// Kahan compensated accumulation: sum - comp is the running total.
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
+  const float y = x - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+// ------------------------------------------------------------ W factors --
+// The reference's sentinel: C abs() of a double truncates to int
+// (Integrand.c:371), so it fires for |x| >= 601; conversions beyond the int
+// range give INT_MIN on x86 (no sentinel), which is mirrored.
+__device__ __forceinline__ bool sentinel600(float x) {
+  const float ax = fabsf(x);
+  return ax >= 601.0f && ax < 2147483648.0f;
+}
+
+// cosh in FP64 range: FP32 coshf below |x| = 80, FP64 exp above (FP32 coshf
+// overflows near 89 while the reference's FP64 cosh is finite to 710).
+__device__ __forceinline__ double cosh_wide(float x) {
+  const float ax = fabsf(x);
+  if (ax < 80.0f) return (double)coshf(ax);
+  return 0.5 * exp((double)ax);
+}
+
+// Per-loop factors of EVMean (Integrand.c:352-390):
+//   w0 = W_N   = cos(phi_x/2 + (phi_y+phi_z)/4) [* cosh(same of psi)]
+//   w1 = W_N/2 = cos(phi_x)                      [* cosh(psi_x)]
+//   w2 = W_N/4 = cos((phi_y+phi_z)/2)            [* cosh(same of psi)]
+template <bool FERM>
+__device__ __forceinline__ void wfactors(float p0, float p1, float p2, float q0, float q1,
+                                         float q2, double &w0, double &w1, double &w2) {
+  const float nb4 = p1 + p2;
+  w0 = (double)cosf(fmaf(0.5f, p0, 0.25f * nb4));
+  w1 = (double)cosf(p0);
+  w2 = (double)cosf(0.5f * nb4);
+  if (FERM) {
+    const float nb4f = q1 + q2;
+    if (sentinel600(nb4f) || sentinel600(q0)) {
+      w0 *= 1.0e10;
+      w1 *= 1.0e10;
+      w2 *= 1.0e10;
+    } else {
+      w0 *= cosh_wide(fmaf(0.5f, q0, 0.25f * nb4f));
+      w1 *= cosh_wide(q0);
+      w2 *= cosh_wide(0.5f * nb4f);
+    }
+  }
+}
+
+// Finishes one loop at one instance (intEV.cu:553-561 and the EVMean
+// factors): G*, H* are the loop's Simpson sums without the h/3 factor and
+// the f' scale; phases are F*G*h/3 and spin exponents 2F T sum/(N/2) resp.
+// 2F T sum/(N/4) (tq = 4T/N).  The W factors of every flux value are added
+// to acc in FP64.
+template <int P, bool FERM>
+__device__ __forceinline__ void loop_epilogue(const float G[3], const float H[3],
+                                              const FieldDev &F, float h3, float tq, int nF,
+                                              const float *Fv, double (&acc)[kMaxF][3]) {
+  const float fs = Profile<P>::fp_scale(F) * h3;
+  const float g0 = G[0] * h3, g1 = G[1] * h3, g2 = G[2] * h3;
+  const float s0 = H[0] * fs * tq, s1 = H[1] * fs * (2.0f * tq), s2 = H[2] * fs * (2.0f * tq);
+#pragma unroll
+  for (int j = 0; j < kMaxF; ++j) {
+    if (j < nF) {
+      const float f = Fv[j];
+      double w0, w1, w2;
+      wfactors<FERM>(f * g0, f * g1, f * g2, f * s0, f * s1, f * s2, w0, w1, w2);
+      acc[j][0] += w0;
+      acc[j][1] += w1;
+      acc[j][2] += w2;
+    }
+  }
+}
+
+// ------------------------------------------ bulk copy + mbarrier (PTX) --
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile(
+      "{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(
+          smem_addr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+// global -> shared bulk copy (non-tensor TMA); addresses 16-byte aligned,
+// size a multiple of 16 bytes; completion is signalled on bar.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Bounded wait on an mbarrier phase: returns false when max_tries polls
+// (each a hardware-suspended try_wait) did not see the phase complete.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint32_t max_tries) {
+  const uint32_t addr = smem_addr(bar);
+  for (uint32_t it = 0; it < max_tries; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, "
+        "1, 0, p; }"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+}  // namespace wl

@@ -1,0 +1,92 @@
+// wl_internal.h -- launch interfaces between the C-ABI runtime (wl_api.cpp)
+// and the kernels (wl_sweep.cu, wl_loopwarp.cu, wl_misc.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "wl_types.h"
+
+namespace wl {
+
+// device-side status codes written to the status word of a launch
+enum : int { kDevOk = 0, kDevTimeout = 1, kDevBadInstance = 2 };
+
+// Instance-parallel sweep: one thread per (instance), one CTA per
+// (instance tile, chunk of loops); the chunk's loops are streamed through a
+// shared-memory ring by bulk copies and every thread walks every point.
+constexpr int kSweepThreads = 128;   // instances per CTA
+constexpr int kSweepStages = 4;      // shared-memory ring depth
+constexpr int kSweepChunkPts = 256;  // points per bulk copy (4 KiB)
+
+struct SweepArgs {
+  const float4 *loops;  // [Nl][ppl]
+  int Nl, ppl;
+  int ninst;
+  const float *cx, *cy;  // [ninst] centre of mass
+  const float *rtT;      // [ninst] float(sqrt(T)) as the reference passes it
+  const float *tq;       // [ninst] 4 T / ppl: spin normalisation 2T/(N/2)
+  int nF;
+  float F[kMaxF];
+  FieldDev field;
+  int chunk_loops;   // loops per CTA
+  int n_chunks;      // Nl / chunk_loops
+  double *partial;   // [n_chunks][nF][3][ninst]
+  int *status;       // kDevOk / kDevTimeout
+  uint32_t wait_tries;
+};
+
+// Loop-parallel sweep: one warp per (loop, instance), lanes over groups of
+// four points; per-loop results.  Used for few instances and for EV().
+constexpr int kLoopWarps = 4;  // warps per CTA
+
+struct LoopArgs {
+  const float4 *loops;
+  int Nl, ppl;
+  int ninst;
+  const float *cx, *cy, *rtT, *tq;
+  int nF;
+  float F[kMaxF];
+  FieldDev field;
+  double *partial;  // [Nl][nF][3][ninst]  (chunk = one loop)
+  float4 *scal;     // optional [ninst][Nl] Wsscal of F[0]
+  float4 *ferm;     // optional [ninst][Nl] Wsferm of F[0]
+};
+
+// returns cudaErrorInvalidValue for an unsupported (profile, nint)
+cudaError_t launch_sweep(int profile, bool fermion, int nint, const SweepArgs &a,
+                         cudaStream_t s);
+cudaError_t launch_loopwarp(int profile, bool fermion, int nint, const LoopArgs &a,
+                            cudaStream_t s);
+
+// partial sums -> per-group <W>, mean and SEM over groups
+cudaError_t launch_group_reduce(const double *partial, int n_chunks, int chunks_per_group,
+                                int loops_per_group, int ninst, int nF, double *out_group,
+                                double *out_mean, double *out_sem, cudaStream_t s);
+
+// EV(): mean over an index list of per-loop W factors (partial with
+// ninst = 1, nF = 1) and the Richardson combination; writes one double.
+cudaError_t launch_list_mean(const double *partial, const int *list, int n, double *out,
+                             cudaStream_t s);
+
+// device-resident instances (cx, cy, T) -> the sweep's float arrays
+// [cx | cy | rtT | tq]; flags T <= 0 or non-finite values in *status
+cudaError_t launch_instance_setup(const double *cx, const double *cy, const double *T,
+                                  int ninst, int ppl, float *out, int *status,
+                                  cudaStream_t s);
+
+// pipe throughput probes: kind 0 FP32 FMA chains, 1 MUFU rcp chains;
+// each thread performs iters * 8 operations
+cudaError_t launch_peak_probe(int kind, int blocks, int threads, int iters, float *sink,
+                              cudaStream_t s);
+
+// seeded unit loops
+cudaError_t launch_vloops(uint64_t seed, int first, int Nl, int ppl, float4 *out,
+                          cudaStream_t s);
+
+// bytes of dynamic shared memory of the sweep kernel
+constexpr size_t sweep_smem_bytes() {
+  return (size_t)kSweepStages * kSweepChunkPts * sizeof(float4);
+}
+
+}  // namespace wl

@@ -1,0 +1,277 @@
+// wl_misc.cu -- profile dispatch, FP64 loop-average reductions and the
+// seeded unit-loop generator.
+#include <math.h>
+
+#include "wl_device.cuh"
+#include "wl_internal.h"
+
+namespace wl {
+
+cudaError_t launch_sweep_smooth(int, bool, int, const SweepArgs *, const LoopArgs *,
+                                cudaStream_t);
+cudaError_t launch_sweep_simple(int, bool, int, const SweepArgs *, const LoopArgs *,
+                                cudaStream_t);
+cudaError_t launch_sweep_periodic(int, bool, int, const SweepArgs *, const LoopArgs *,
+                                  cudaStream_t);
+cudaError_t launch_sweep_fixflux(int, bool, int, const SweepArgs *, const LoopArgs *,
+                                 cudaStream_t);
+
+static cudaError_t dispatch(int profile, bool fermion, int nint, const SweepArgs *sa,
+                            const LoopArgs *la, cudaStream_t s) {
+  switch (profile) {
+    case kSmooth: return launch_sweep_smooth(profile, fermion, nint, sa, la, s);
+    case kStep:
+    case kQuadratic:
+    case kGaussian: return launch_sweep_simple(profile, fermion, nint, sa, la, s);
+    case kPeriodic: return launch_sweep_periodic(profile, fermion, nint, sa, la, s);
+    case kFixflux:
+    case kFixfluxFF: return launch_sweep_fixflux(profile, fermion, nint, sa, la, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_sweep(int profile, bool fermion, int nint, const SweepArgs &a,
+                         cudaStream_t s) {
+  return dispatch(profile, fermion, nint, &a, nullptr, s);
+}
+
+cudaError_t launch_loopwarp(int profile, bool fermion, int nint, const LoopArgs &a,
+                            cudaStream_t s) {
+  return dispatch(profile, fermion, nint, nullptr, &a, s);
+}
+
+// ---------------------------------------------------------- reductions --
+// One thread per (instance, flux value): group sums over the group's chunks
+// in chunk order (the result of an instance does not depend on how many
+// other instances share the launch), the Richardson combination
+// 8/3 W_N - 2 W_N/2 + 1/3 W_N/4 (Integrand.c:400), then mean and standard
+// error over the groups.
+__global__ void group_reduce_kernel(const double *__restrict__ partial, int n_chunks,
+                                    int cpg, int lpg, int ninst, int nF,
+                                    double *__restrict__ out_group,
+                                    double *__restrict__ out_mean,
+                                    double *__restrict__ out_sem) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= ninst * nF) return;
+  const int inst = idx % ninst, j = idx / ninst;
+  const int ng = n_chunks / cpg;
+  const double inv = 1.0 / (double)lpg;
+  auto group_value = [&](int g) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int c = g * cpg; c < (g + 1) * cpg; ++c) {
+      const size_t base = ((size_t)(c * nF + j) * 3) * ninst + inst;
+      s0 += partial[base];
+      s1 += partial[base + ninst];
+      s2 += partial[base + 2 * (size_t)ninst];
+    }
+    return 8.0 / 3.0 * (s0 * inv) - 2.0 * (s1 * inv) + 1.0 / 3.0 * (s2 * inv);
+  };
+  double mean = 0.0;
+  for (int g = 0; g < ng; ++g) {
+    const double v = group_value(g);
+    if (out_group) out_group[((size_t)inst * nF + j) * ng + g] = v;
+    mean += v;
+  }
+  mean /= (double)ng;
+  double ss = 0.0;
+  for (int g = 0; g < ng; ++g) {
+    const double v = out_group ? out_group[((size_t)inst * nF + j) * ng + g] : group_value(g);
+    ss += (v - mean) * (v - mean);
+  }
+  if (out_mean) out_mean[(size_t)inst * nF + j] = mean;
+  if (out_sem)
+    out_sem[(size_t)inst * nF + j] = ng > 1 ? sqrt(ss / ((double)ng * (ng - 1.0))) : 0.0;
+}
+
+cudaError_t launch_group_reduce(const double *partial, int n_chunks, int cpg, int lpg,
+                                int ninst, int nF, double *out_group, double *out_mean,
+                                double *out_sem, cudaStream_t s) {
+  const int n = ninst * nF, bs = 128;
+  group_reduce_kernel<<<(n + bs - 1) / bs, bs, 0, s>>>(partial, n_chunks, cpg, lpg, ninst,
+                                                        nF, out_group, out_mean, out_sem);
+  return cudaGetLastError();
+}
+
+// EV(): mean of the per-loop factors over an index list, fixed-order tree.
+constexpr int kListThreads = 128;
+__global__ void __launch_bounds__(kListThreads)
+    list_mean_kernel(const double *__restrict__ w, const int *__restrict__ list, int n,
+                     double *__restrict__ out) {
+  __shared__ double red[3][kListThreads];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += kListThreads) {
+    const int l = list[i];
+    s0 += w[3 * (size_t)l];
+    s1 += w[3 * (size_t)l + 1];
+    s2 += w[3 * (size_t)l + 2];
+  }
+  red[0][threadIdx.x] = s0;
+  red[1][threadIdx.x] = s1;
+  red[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int h = kListThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int r = 0; r < 3; ++r) red[r][threadIdx.x] += red[r][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double inv = 1.0 / (double)n;
+    out[0] = 8.0 / 3.0 * (red[0][0] * inv) - 2.0 * (red[1][0] * inv) +
+             1.0 / 3.0 * (red[2][0] * inv);
+  }
+}
+
+cudaError_t launch_list_mean(const double *partial, const int *list, int n, double *out,
+                             cudaStream_t s) {
+  list_mean_kernel<<<1, kListThreads, 0, s>>>(partial, list, n, out);
+  return cudaGetLastError();
+}
+
+// instance set-up on the device: the same float conversions as the host path
+// (rtT = float(sqrt(T)), tq = float(4T/ppl))
+__global__ void instance_setup_kernel(const double *__restrict__ cx,
+                                      const double *__restrict__ cy,
+                                      const double *__restrict__ T, int ninst, int ppl,
+                                      float *__restrict__ out, int *__restrict__ status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ninst) return;
+  const double x = cx[i], y = cy[i], t = T[i];
+  const bool ok = isfinite(x) && isfinite(y) && isfinite(t) && t > 0.0;
+  if (!ok) atomicExch(status, kDevBadInstance);
+  const double tt = ok ? t : 1.0;
+  out[i] = ok ? (float)x : 0.0f;
+  out[ninst + i] = ok ? (float)y : 0.0f;
+  out[2 * ninst + i] = (float)sqrt(tt);
+  out[3 * ninst + i] = (float)(4.0 * tt / (double)ppl);
+}
+
+cudaError_t launch_instance_setup(const double *cx, const double *cy, const double *T,
+                                  int ninst, int ppl, float *out, int *status,
+                                  cudaStream_t s) {
+  const int bs = 256;
+  instance_setup_kernel<<<(ninst + bs - 1) / bs, bs, 0, s>>>(cx, cy, T, ninst, ppl, out,
+                                                             status);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ probes --
+// Eight independent dependency chains per thread keep the pipe busy; the
+// result is stored only if it is impossible, so the work cannot be removed.
+__global__ void peak_fma_kernel(int iters, float *sink) {
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1.0f + 1e-7f * (float)(threadIdx.x + k);
+  const float m = 0.999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == -1.0f) sink[blockIdx.x] = s;
+}
+
+__global__ void peak_rcp_kernel(int iters, float *sink) {
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1.5f + 1e-3f * (float)(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = rcp_fast(a[k]);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == -1.0f) sink[blockIdx.x] = s;
+}
+
+cudaError_t launch_peak_probe(int kind, int blocks, int threads, int iters, float *sink,
+                              cudaStream_t s) {
+  if (kind == 0)
+    peak_fma_kernel<<<blocks, threads, 0, s>>>(iters, sink);
+  else
+    peak_rcp_kernel<<<blocks, threads, 0, s>>>(iters, sink);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------ unit-loop ensemble --
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11): 10 rounds of the multiply-xor bijection with
+// Weyl-sequence key schedule.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k.x += 0x9E3779B9u;
+      k.y += 0xBB67AE85u;
+    }
+    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+  }
+  return c;
+}
+
+constexpr uint32_t kVloopTag = 0x764C6F6Fu;  // counter word 2 ("vLoo")
+
+// four standard normals of step k of loop l (Box-Muller in FP64)
+__device__ __forceinline__ void step_normals(uint2 key, int k, int lg, double n[4]) {
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)k, (uint32_t)lg, kVloopTag, 0u), key);
+  const double two32 = 4294967296.0;
+  const uint32_t v[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const double u = ((double)v[2 * p] + 0.5) / two32;
+    const double w = ((double)v[2 * p + 1] + 0.5) / two32;
+    const double rad = sqrt(-2.0 * log(u));
+    double sn, cs;
+    sincospi(2.0 * w, &sn, &cs);
+    n[2 * p] = rad * cs;
+    n[2 * p + 1] = rad * sn;
+  }
+}
+
+// One thread per loop.  A discrete Brownian bridge of unit proper time:
+// increments N(0, 2/N) per component (the kinetic weight exp(-1/4 int xdot^2)
+// of a unit loop), x_k = y_k - (k/N) y_N, then the mean is removed.  Two
+// passes over the same counter-based draws avoid storing the walk.
+__global__ void vloops_kernel(uint64_t seed, int first, int Nl, int ppl,
+                              float4 *__restrict__ out) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= Nl) return;
+  const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+  const double sigma = sqrt(2.0 / (double)ppl);
+  double y[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0};
+  for (int k = 0; k < ppl; ++k) {
+    double n[4];
+    step_normals(key, k, first + l, n);
+    for (int d = 0; d < 4; ++d) {
+      sy[d] += y[d];
+      y[d] += sigma * n[d];
+    }
+  }
+  // mean of x_k = (1/N) sum y_k - y_N (N-1)/(2N)
+  double mean[4];
+  for (int d = 0; d < 4; ++d)
+    mean[d] = sy[d] / (double)ppl - y[d] * ((double)(ppl - 1) / (2.0 * ppl));
+  double yy[4] = {0, 0, 0, 0};
+  float4 *o = out + (size_t)l * ppl;
+  for (int k = 0; k < ppl; ++k) {
+    const double fk = (double)k / (double)ppl;
+    o[k] = make_float4((float)(yy[0] - fk * y[0] - mean[0]), (float)(yy[1] - fk * y[1] - mean[1]),
+                       (float)(yy[2] - fk * y[2] - mean[2]), (float)(yy[3] - fk * y[3] - mean[3]));
+    double n[4];
+    step_normals(key, k, first + l, n);
+    for (int d = 0; d < 4; ++d) yy[d] += sigma * n[d];
+  }
+}
+
+cudaError_t launch_vloops(uint64_t seed, int first, int Nl, int ppl, float4 *out,
+                          cudaStream_t s) {
+  const int bs = 64;
+  vloops_kernel<<<(Nl + bs - 1) / bs, bs, 0, s>>>(seed, first, Nl, ppl, out);
+  return cudaGetLastError();
+}
+
+}  // namespace wl

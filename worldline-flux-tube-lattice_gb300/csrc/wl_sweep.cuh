@@ -1,0 +1,295 @@
+// wl_sweep.cuh -- the two Wilson-loop sweep kernels.
+//
+// Both compute, per (loop, instance), the reference kernel's per-loop phases
+// (ExpectValue -> WilsonLoop, intEV.cu:508-582) and the EVMean factors
+// (Integrand.c:352-390), and write FP64 partial sums of the W factors.
+//
+// sweep_kernel (instance-parallel): thread = instance (centre of mass,
+//   proper time), CTA = 128 instances x a chunk of loops.  The chunk's loops
+//   are streamed through a 4-stage shared-memory ring with bulk copies
+//   (cp.async.bulk + mbarrier); every thread walks every point of the staged
+//   loop, so each shared-memory load is a warp-wide broadcast and the loop
+//   data is read from HBM once per CTA.  Within a loop the points are visited
+//   in order; the three sub-loops (N/2: odd points, N/4a: i = 0 mod 4,
+//   N/4b: i = 2 mod 4; intEV.cu:461-506) advance together, one group of four
+//   points (four segments) at a time, and each segment adds to its sub-loop
+//   in the reference's order.  Phases accumulate in FP32 with Kahan
+//   compensation per block of 8 groups; W factors accumulate in FP64.
+//
+// loopwarp_kernel (loop-parallel): warp = (loop, instance), lanes over the
+//   groups of four points; per-loop results (EV() and few-instance calls).
+#pragma once
+
+#include "wl_device.cuh"
+#include "wl_internal.h"
+
+namespace wl {
+
+template <int P, bool FERM, int NINT>
+__global__ void __launch_bounds__(kSweepThreads)
+    sweep_kernel(const __grid_constant__ SweepArgs A) {
+  extern __shared__ __align__(128) float4 ring[];  // [kSweepStages][kSweepChunkPts]
+  __shared__ __align__(8) uint64_t full_bar[kSweepStages];
+  __shared__ int sm_bad;
+
+  const int tid = threadIdx.x;
+  const int inst = blockIdx.x * kSweepThreads + tid;
+  const int ic = inst < A.ninst ? inst : A.ninst - 1;
+  const int chunk = blockIdx.y;
+  const int l0 = chunk * A.chunk_loops;
+  const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
+  const int K = A.chunk_loops * nck;
+
+  const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic], tq = A.tq[ic];
+  const FieldDev &F = A.field;
+  const float h3 = (NINT > 0 ? 1.0f / (float)NINT : F.h) * (1.0f / 3.0f);
+
+  if (tid == 0) {
+    for (int st = 0; st < kSweepStages; ++st) mbar_init(&full_bar[st], 1);
+    fence_mbar_init();
+    sm_bad = 0;
+  }
+  __syncthreads();
+
+  auto issue = [&](int k) {  // chunk k -> stage k % kSweepStages
+    const int st = k % kSweepStages;
+    const int l = l0 + k / nck, c = k % nck;
+    const int p0 = c * kSweepChunkPts;
+    const int np = min(kSweepChunkPts, A.ppl - p0);
+    const uint32_t bytes = (uint32_t)np * (uint32_t)sizeof(float4);
+    mbar_arrive_expect_tx(&full_bar[st], bytes);
+    bulk_g2s(ring + st * kSweepChunkPts, A.loops + (size_t)l * A.ppl + p0, bytes,
+             &full_bar[st]);
+  };
+  if (tid == 0)
+    for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
+
+  double acc[kMaxF][3];
+#pragma unroll
+  for (int j = 0; j < kMaxF; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0;
+
+  // running sums of the current loop: phase and spin, each with compensation
+  float ph[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
+  float sp[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
+  // previous point of each sub-loop and the first points (closing segments)
+  float zAx = 0.f, zAy = 0.f, zBx = 0.f, zBy = 0.f, zOx = 0.f, zOy = 0.f;
+  float z0x = 0.f, z0y = 0.f, z1x = 0.f, z1y = 0.f, z2x = 0.f, z2y = 0.f;
+
+  int k = 0;
+  for (; k < K; ++k) {
+    const int st = k % kSweepStages;
+    const uint32_t par = (uint32_t)(k / kSweepStages) & 1u;
+    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) sm_bad = 1;
+
+    const int c = k % nck;
+    const int p0 = c * kSweepChunkPts;
+    const int p1 = min(A.ppl, p0 + kSweepChunkPts);
+    const float2 *pts = reinterpret_cast<const float2 *>(ring + st * kSweepChunkPts);
+    auto pt = [&](int p, float &x, float &y) {
+      const float2 v = pts[2 * (p - p0)];  // (x, y) of the float4 point
+      x = fmaf(s, v.x, cx);
+      y = fmaf(s, v.y, cy);
+    };
+
+    int q = p0 >> 2;
+    const int qend = p1 >> 2;
+    if (c == 0) {  // first chunk of a loop: points 0..3 open the sub-loops
+#pragma unroll
+      for (int r = 0; r < 3; ++r) ph[r] = pc[r] = sp[r] = sc[r] = 0.f;
+      float z3x, z3y;
+      pt(0, z0x, z0y);
+      pt(1, z1x, z1y);
+      pt(2, z2x, z2y);
+      pt(3, z3x, z3y);
+      segment<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, ph[0], sp[0]);  // N/2: 1 -> 3
+      zAx = z0x; zAy = z0y;
+      zBx = z2x; zBy = z2y;
+      zOx = z3x; zOy = z3y;
+      q = 1;
+    }
+    while (q < qend) {
+      const int qe = min(q + 8, qend);
+      float bp0 = 0.f, bp1 = 0.f, bp2 = 0.f, bs0 = 0.f, bs1 = 0.f, bs2 = 0.f;
+      auto group = [&](int qq) {
+        float P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
+        pt(4 * qq, P0x, P0y);
+        pt(4 * qq + 1, P1x, P1y);
+        pt(4 * qq + 2, P2x, P2y);
+        pt(4 * qq + 3, P3x, P3y);
+        segment<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, bp2, bs2);  // N/4a: 4q-4 -> 4q
+        segment<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, bp0, bs0);  // N/2 : 4q-1 -> 4q+1
+        segment<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, bp1, bs1);  // N/4b: 4q-2 -> 4q+2
+        segment<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, bp0, bs0);  // N/2 : 4q+1 -> 4q+3
+        zAx = P0x; zAy = P0y;
+        zBx = P2x; zBy = P2y;
+        zOx = P3x; zOy = P3y;
+      };
+      if constexpr (Profile<P>::kHeavy) {
+#pragma unroll 1
+        for (; q < qe; ++q) group(q);
+      } else {
+#pragma unroll 2
+        for (; q < qe; ++q) group(q);
+      }
+      kahan_add(ph[0], pc[0], bp0);
+      kahan_add(ph[1], pc[1], bp1);
+      kahan_add(ph[2], pc[2], bp2);
+      if (FERM) {
+        kahan_add(sp[0], sc[0], bs0);
+        kahan_add(sp[1], sc[1], bs1);
+        kahan_add(sp[2], sc[2], bs2);
+      }
+    }
+
+    if (c == nck - 1) {  // last chunk: closing segments back to points 1, 0, 2
+      float tp0 = 0.f, tp1 = 0.f, tp2 = 0.f, ts0 = 0.f, ts1 = 0.f, ts2 = 0.f;
+      segment<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, tp0, ts0);  // N/2 : N-1 -> 1
+      segment<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, tp1, ts1);  // N/4b: N-2 -> 2
+      segment<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, tp2, ts2);  // N/4a: N-4 -> 0
+      kahan_add(ph[0], pc[0], tp0);
+      kahan_add(ph[1], pc[1], tp1);
+      kahan_add(ph[2], pc[2], tp2);
+      kahan_add(sp[0], sc[0], ts0);
+      kahan_add(sp[1], sc[1], ts1);
+      kahan_add(sp[2], sc[2], ts2);
+      const float G[3] = {ph[0] - pc[0], ph[1] - pc[1], ph[2] - pc[2]};
+      const float H[3] = {sp[0] - sc[0], sp[1] - sc[1], sp[2] - sc[2]};
+      loop_epilogue<P, FERM>(G, H, F, h3, tq, A.nF, A.F, acc);
+    }
+
+    __syncthreads();  // every thread is done with stage st
+    if (sm_bad) break;
+    if (tid == 0 && k + kSweepStages < K) issue(k + kSweepStages);
+  }
+
+  if (sm_bad) {
+    // a copy did not arrive in time: wait (bounded) for the copies still in
+    // flight so that none lands after the CTA exits, report, write nothing
+    if (tid == 0) {
+      const int kend = min(K, k + kSweepStages);
+      for (int kk = k; kk < kend; ++kk)
+        mbar_wait_bounded(&full_bar[kk % kSweepStages], (uint32_t)(kk / kSweepStages) & 1u,
+                          A.wait_tries);
+      atomicExch(A.status, kDevTimeout);
+    }
+    return;
+  }
+
+  if (inst < A.ninst) {
+#pragma unroll
+    for (int j = 0; j < kMaxF; ++j)
+      if (j < A.nF)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          A.partial[((size_t)(chunk * A.nF + j) * 3 + r) * A.ninst + inst] = acc[j][r];
+  }
+}
+
+template <int P, bool FERM, int NINT>
+__global__ void __launch_bounds__(kLoopWarps * 32)
+    loopwarp_kernel(const __grid_constant__ LoopArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int l = blockIdx.x * kLoopWarps + (threadIdx.x >> 5);
+  const int inst = blockIdx.y;
+  if (l >= A.Nl) return;  // whole warp
+  const float cx = A.cx[inst], cy = A.cy[inst], s = A.rtT[inst], tq = A.tq[inst];
+  const FieldDev &F = A.field;
+  const float2 *w = reinterpret_cast<const float2 *>(A.loops + (size_t)l * A.ppl);
+  auto pt = [&](int p, float &x, float &y) {
+    const float2 v = __ldg(&w[2 * p]);
+    x = fmaf(s, v.x, cx);
+    y = fmaf(s, v.y, cy);
+  };
+  // group q covers points 4q..4q+3 and the four segments ending there; the
+  // previous points of group 0 wrap to the end of the loop (closing segments)
+  const int nq = A.ppl >> 2;
+  float ph[3] = {0.f, 0.f, 0.f}, sp[3] = {0.f, 0.f, 0.f};
+  for (int q = lane; q < nq; q += 32) {
+    const int pa = (q == 0 ? A.ppl : 4 * q) - 4;
+    float zAx, zAy, zBx, zBy, zOx, zOy, P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
+    pt(pa, zAx, zAy);
+    pt(pa + 2, zBx, zBy);
+    pt(pa + 3, zOx, zOy);
+    pt(4 * q, P0x, P0y);
+    pt(4 * q + 1, P1x, P1y);
+    pt(4 * q + 2, P2x, P2y);
+    pt(4 * q + 3, P3x, P3y);
+    segment<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, ph[2], sp[2]);
+    segment<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, ph[0], sp[0]);
+    segment<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, ph[1], sp[1]);
+    segment<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, ph[0], sp[0]);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      ph[r] += __shfl_xor_sync(0xffffffffu, ph[r], off);
+      if (FERM) sp[r] += __shfl_xor_sync(0xffffffffu, sp[r], off);
+    }
+  }
+  if (lane == 0) {
+    const float h3 = (NINT > 0 ? 1.0f / (float)NINT : F.h) * (1.0f / 3.0f);
+    double acc[kMaxF][3];
+#pragma unroll
+    for (int j = 0; j < kMaxF; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0;
+    loop_epilogue<P, FERM>(ph, sp, F, h3, tq, A.nF, A.F, acc);
+#pragma unroll
+    for (int j = 0; j < kMaxF; ++j)
+      if (j < A.nF)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          A.partial[((size_t)(l * A.nF + j) * 3 + r) * A.ninst + inst] = acc[j][r];
+    const size_t o = (size_t)inst * A.Nl + l;
+    if (A.scal) A.scal[o] = make_float4(A.F[0] * ph[0] * h3, A.F[0] * ph[1] * h3,
+                                        A.F[0] * ph[2] * h3, 0.0f);
+    if (FERM && A.ferm) {
+      const float fs = Profile<P>::fp_scale(F) * h3 * A.F[0];
+      A.ferm[o] = make_float4(sp[0] * fs * tq, sp[1] * fs * 2.0f * tq,
+                              sp[2] * fs * 2.0f * tq, 0.0f);
+    }
+  }
+}
+
+// instantiation + dispatch over (fermion, nint) for one profile
+template <int P>
+cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStream_t s) {
+  const dim3 grid((a.ninst + kSweepThreads - 1) / kSweepThreads, a.n_chunks);
+  const size_t smem = sweep_smem_bytes();
+#define WL_SWEEP_CASE(FE, NI)                                                      \
+  if (fermion == FE && (NI == 0 || nint == NI)) {                                  \
+    sweep_kernel<P, FE, NI><<<grid, kSweepThreads, smem, s>>>(a);                  \
+    return cudaGetLastError();                                                     \
+  }
+  if constexpr (!Profile<P>::kHeavy) {
+    WL_SWEEP_CASE(true, 4)
+    WL_SWEEP_CASE(false, 4)
+    WL_SWEEP_CASE(true, 50)
+    WL_SWEEP_CASE(false, 50)
+  }
+  WL_SWEEP_CASE(true, 0)
+  WL_SWEEP_CASE(false, 0)
+#undef WL_SWEEP_CASE
+  return cudaErrorInvalidValue;
+}
+
+template <int P>
+cudaError_t loopwarp_dispatch(bool fermion, int nint, const LoopArgs &a, cudaStream_t s) {
+  const dim3 grid((a.Nl + kLoopWarps - 1) / kLoopWarps, a.ninst);
+#define WL_LOOP_CASE(FE, NI)                                                       \
+  if (fermion == FE && (NI == 0 || nint == NI)) {                                  \
+    loopwarp_kernel<P, FE, NI><<<grid, kLoopWarps * 32, 0, s>>>(a);                \
+    return cudaGetLastError();                                                     \
+  }
+  if constexpr (!Profile<P>::kHeavy) {
+    WL_LOOP_CASE(true, 4)
+    WL_LOOP_CASE(false, 4)
+    WL_LOOP_CASE(true, 50)
+    WL_LOOP_CASE(false, 50)
+  }
+  WL_LOOP_CASE(true, 0)
+  WL_LOOP_CASE(false, 0)
+#undef WL_LOOP_CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace wl

@@ -1,0 +1,32 @@
+// wl_types.h -- types and constants shared by host runtime and kernels.
+#pragma once
+
+#include <stdint.h>
+
+namespace wl {
+
+enum : int {
+  kStep = 0,
+  kSmooth = 1,
+  kQuadratic = 2,
+  kGaussian = 3,
+  kPeriodic = 4,
+  kFixflux = 6,
+  kFixfluxFF = 7  // fixflux with the intEVff.cu phi/chi fits
+};
+
+constexpr int kMaxF = 4;  // flux values sharing one geometric pass
+
+// Field constants of one launch, FP32 (the reference kernel is FP32).
+struct FieldDev {
+  float l2, inv_l2, lam;  // lambda^2, 1/lambda^2, lambda
+  float a, lmin;          // lattice spacing, fixflux minimum width
+  float lml, aml;         // fixflux (lam-lmin)/(a-lmin), (a-lam)/(a-lmin)
+  // clamps of the segment polynomial: the reference's 1e-8 / 1e-10
+  // (intEV.cu:418-422, 439) or -inf / 1e-30 in exact mode
+  float clampA, clampB, clampC, clampE, clampI;
+  int nint;  // Simpson intervals (used by the run-time-n kernels)
+  float h;   // 1.0f / nint
+};
+
+}  // namespace wl

@@ -1,0 +1,257 @@
+"""Python host binding of libwlgpu.so, the GB300 Wilson-loop library.
+
+A thin ctypes layer over the C ABI of include/wlgpu.h and include/wl_legacy.h.
+It mirrors the reference's host interface for the path: ``Wparams`` and
+``EV(T, params, WLlist)`` (intEV.cu:111-148) plus the batched API.  There is
+no CPU fallback: importing raises if the CUDA library is missing, and every
+call raises ``WlError`` on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libwlgpu.so")
+
+PROFILES = {"step": 0, "smooth": 1, "quadratic": 2, "gaussian": 3, "periodic": 4,
+            "fixflux": 6}
+MODE_REFCOMPAT, MODE_EXACT = 0, 1
+STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
+          -4: "device wait timed out", -5: "unknown handle", -6: "admission rejected"}
+
+
+class WlError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__("%s (%d)%s" % (STATUS.get(status, "error"), status,
+                                        (": " + msg) if msg else ""))
+        self.status = status
+
+
+class Field(C.Structure):
+    """wl_field of wlgpu.h."""
+    _fields_ = [("profile", C.c_int), ("fermion", C.c_int), ("nint", C.c_int),
+                ("mode", C.c_int), ("ff_variant", C.c_int), ("reserved", C.c_int),
+                ("lambda2", C.c_double), ("tubedist", C.c_double), ("lmin", C.c_double)]
+
+
+def field(profile="smooth", fermion=0, nint=50, mode=MODE_REFCOMPAT, lambda2=1.0,
+          tubedist=1.0, lmin=None, ff_variant=0) -> Field:
+    if isinstance(profile, str):
+        profile = PROFILES[profile]
+    if lmin is None:
+        lmin = 0.1 * tubedist
+    return Field(profile, int(fermion), int(nint), int(mode), int(ff_variant), 0,
+                 float(lambda2), float(tubedist), float(lmin))
+
+
+class Float4(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("w", C.c_float)]
+
+
+class Wparams(C.Structure):
+    """struct Wparams of wl_legacy.h (the reference's intT.h)."""
+    _fields_ = [("Nl", C.c_int), ("Nppl", C.c_int), ("F", C.c_double), ("l2", C.c_double),
+                ("xcm", Float4), ("Wsscal_h", C.c_void_p), ("Wsscal_d", C.c_void_p),
+                ("Wsferm_h", C.c_void_p), ("Wsferm_d", C.c_void_p),
+                ("worldlines", C.c_void_p), ("SE", C.c_double), ("nBlocks", C.c_int),
+                ("nThreads", C.c_int), ("ng", C.c_int), ("fermion", C.c_int),
+                ("flcoefs", C.c_void_p), ("rho2sp", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libwlgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libwlgpu.so is not built (%s); run build.py" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp, fp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), \
+            C.POINTER(C.c_float)
+        L.wl_version.restype = C.c_char_p
+        L.wl_status_string.restype = C.c_char_p
+        L.wl_status_string.argtypes = [C.c_int]
+        L.wl_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+        L.wl_ctx_destroy.argtypes = [vp]
+        L.wl_last_error.argtypes = [vp, C.c_char_p, C.c_int]
+        L.wl_ctx_synchronize.argtypes = [vp]
+        L.wl_ensemble_upload.argtypes = [vp, fp, C.c_int, C.c_int, ip]
+        L.wl_ensemble_wrap.argtypes = [vp, vp, C.c_int, C.c_int, ip]
+        L.wl_ensemble_generate.argtypes = [vp, C.c_uint64, C.c_int, C.c_int, C.c_int, ip]
+        L.wl_ensemble_download.argtypes = [vp, C.c_int, fp]
+        L.wl_ensemble_release.argtypes = [vp, C.c_int]
+        L.wl_ensemble_info.argtypes = [vp, C.c_int, C.POINTER(vp), ip, ip]
+        L.wl_eval.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, dp, dp, C.c_int,
+                              dp, C.c_int, dp, dp, dp]
+        L.wl_eval_device.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, vp, vp, vp,
+                                     C.c_int, dp, C.c_int, vp, vp, vp]
+        L.wl_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+        L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
+        L.wl_loops.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_double,
+                               C.c_double, C.c_double, fp, fp]
+        L.wl_last_launches.argtypes = [vp, ip, C.POINTER(C.c_char_p)]
+        L.wl_legacy_configure.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int]
+        L.EV.restype = C.c_double
+        L.EV.argtypes = [C.c_double, C.c_void_p, ip]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return np.ascontiguousarray(np.atleast_1d(a), dtype=np.float64)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Context:
+    """One device and one stream (wl_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        st = lib().wl_ctx_create(device, C.byref(self._h))
+        if st != 0:
+            raise WlError(st, "wl_ctx_create(%d)" % device)
+
+    def close(self):
+        if self._h:
+            lib().wl_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st):
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            lib().wl_last_error(self._h, buf, 512)
+            raise WlError(st, buf.value.decode())
+
+    def upload(self, loops: np.ndarray) -> int:
+        loops = np.ascontiguousarray(loops, dtype=np.float32)
+        Nl, ppl = loops.shape[:2]
+        h = C.c_int()
+        self._check(lib().wl_ensemble_upload(self._h, _p(loops, C.c_float), Nl, ppl,
+                                             C.byref(h)))
+        return h.value
+
+    def wrap(self, dev_ptr: int, Nl: int, ppl: int) -> int:
+        h = C.c_int()
+        self._check(lib().wl_ensemble_wrap(self._h, C.c_void_p(dev_ptr), Nl, ppl, C.byref(h)))
+        return h.value
+
+    def generate(self, seed: int, Nl: int, ppl: int, first: int = 0) -> int:
+        h = C.c_int()
+        self._check(lib().wl_ensemble_generate(self._h, seed, first, Nl, ppl, C.byref(h)))
+        return h.value
+
+    def download(self, handle: int) -> np.ndarray:
+        Nl, ppl = C.c_int(), C.c_int()
+        self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), C.byref(ppl)))
+        out = np.empty((Nl.value, ppl.value, 4), dtype=np.float32)
+        self._check(lib().wl_ensemble_download(self._h, handle, _p(out, C.c_float)))
+        return out
+
+    def release(self, handle: int):
+        self._check(lib().wl_ensemble_release(self._h, handle))
+
+    def eval(self, handle: int, fld: Field, cx, cy, T, F, group: int = 128,
+             want_groups: bool = True):
+        """<W> per group, mean and SEM: arrays [ninst][nF][ng], [ninst][nF] x2."""
+        cx, cy, T, F = _d(cx), _d(cy), _d(T), _d(F)
+        n = len(T)
+        Nl = C.c_int()
+        self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), None))
+        ng = Nl.value // group if group > 0 else 0
+        groups = np.empty((n, len(F), max(ng, 1))) if want_groups else None
+        mean = np.empty((n, len(F)))
+        sem = np.empty((n, len(F)))
+        self._check(lib().wl_eval(
+            self._h, handle, C.byref(fld), n, _p(cx, C.c_double), _p(cy, C.c_double),
+            _p(T, C.c_double), len(F), _p(F, C.c_double), group,
+            _p(groups, C.c_double) if want_groups else None, _p(mean, C.c_double),
+            _p(sem, C.c_double)))
+        return groups, mean, sem
+
+    def eval_device(self, handle: int, fld: Field, ninst: int, dev_cx: int, dev_cy: int,
+                    dev_T: int, F, group: int = 128, dev_out_group: int = 0,
+                    dev_out_mean: int = 0, dev_out_sem: int = 0):
+        """Asynchronous evaluation on device-resident instance arrays (FP64
+        device pointers given as integers); call synchronize() for the status."""
+        F = _d(F)
+        self._check(lib().wl_eval_device(
+            self._h, handle, C.byref(fld), ninst, C.c_void_p(dev_cx), C.c_void_p(dev_cy),
+            C.c_void_p(dev_T), len(F), _p(F, C.c_double), group,
+            C.c_void_p(dev_out_group or None), C.c_void_p(dev_out_mean or None),
+            C.c_void_p(dev_out_sem or None)))
+
+    def peak_probe(self, kind: int) -> float:
+        """Lane operations per second of the FP32 FMA (0) or MUFU rcp (1) pipe."""
+        v = C.c_double()
+        self._check(lib().wl_peak_probe(self._h, kind, C.byref(v)))
+        return v.value
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer."""
+        s = C.c_void_p()
+        self._check(lib().wl_ctx_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def loops(self, handle: int, fld: Field, cx: float, cy: float, T: float, F: float):
+        """Per-loop Wsscal / Wsferm of one instance: two float32 arrays [Nl][4]."""
+        Nl = C.c_int()
+        self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), None))
+        s = np.empty((Nl.value, 4), dtype=np.float32)
+        f = np.empty((Nl.value, 4), dtype=np.float32)
+        self._check(lib().wl_loops(self._h, handle, C.byref(fld), cx, cy, T, F,
+                                   _p(s, C.c_float), _p(f, C.c_float)))
+        return s, f
+
+    def last_launches(self):
+        n, k = C.c_int(), C.c_char_p()
+        self._check(lib().wl_last_launches(self._h, C.byref(n), C.byref(k)))
+        return n.value, k.value.decode()
+
+    def synchronize(self):
+        self._check(lib().wl_ctx_synchronize(self._h))
+
+
+def legacy_configure(profile="smooth", tubedist=1.0, lmin=None, nint=50,
+                     mode=MODE_REFCOMPAT):
+    if isinstance(profile, str):
+        profile = PROFILES[profile]
+    if lmin is None:
+        lmin = 0.1 * tubedist
+    st = lib().wl_legacy_configure(profile, tubedist, lmin, nint, mode)
+    if st != 0:
+        raise WlError(st, "wl_legacy_configure")
+
+
+def EV(T: float, params: Wparams, WLlist) -> float:
+    """The reference's EV(T, p, WLlist) through the C ABI."""
+    wl = np.ascontiguousarray(WLlist, dtype=np.int32)
+    return lib().EV(T, C.cast(C.pointer(params), C.c_void_p), _p(wl, C.c_int))
+
+
+def version() -> str:
+    return lib().wl_version().decode()
