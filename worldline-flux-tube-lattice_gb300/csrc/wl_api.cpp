@@ -202,7 +202,9 @@ int upload_instances(wl_ctx *ctx, int ninst, const double *cx, const double *cy,
 int plan_chunk(wl_ctx *ctx, int ninst, int Nl, int group) {
   const long tiles = (ninst + wl::kSweepThreads - 1) / wl::kSweepThreads;
   int lc = group;
-  while (lc % 2 == 0 && lc > 1 && tiles * (long)(Nl / lc) < 12L * ctx->num_sms) lc /= 2;
+  while (lc % 2 == 0 && lc > 1 && tiles * (long)(Nl / lc) < 12L * ctx->num_sms &&
+         Nl / (lc / 2) <= 65535)
+    lc /= 2;
   return lc;
 }
 
@@ -464,6 +466,8 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
   if (use_sweep) {
     const int lc = plan_chunk(ctx, ninst, e.Nl, group);
     n_chunks = e.Nl / lc;
+    if (n_chunks > 65535)
+      return fail(ctx, WL_ERR_INVALID, "group %d too small for Nl = %d (grid limit)", group, e.Nl);
     cpg = group / lc;
   } else {
     n_chunks = e.Nl;
