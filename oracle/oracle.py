@@ -85,7 +85,7 @@ def lib():
         L.wlo64_evmean.argtypes = [dp, dp, C.c_int, ip, C.c_int]
         for name in ("wlo64_eval", "wlo32_eval"):
             getattr(L, name).argtypes = [fp, C.c_int, C.c_int, C.c_int, dp, dp, dp, C.c_int,
-                                         dp, Fp, C.c_int, dp, C.c_int]
+                                         dp, Fp, C.c_int, dp, dp, C.c_int]
         Qp = C.POINTER(Qed)
         L.wlo_magfield.restype = C.c_double
         L.wlo_magfield.argtypes = [C.c_double, C.c_double, Fp, Qp]
@@ -179,8 +179,10 @@ def evmean(scal, ferm, WL, fermion):
                               _ptr(wl, C.c_int), fermion)
 
 
-def eval_groups(loops, cx, cy, T, F, fld, group=128, fp32=False, nthreads=0):
-    """Per-group <W>: array [ninst][nF][Nl//group]."""
+def eval_groups(loops, cx, cy, T, F, fld, group=128, fp32=False, nthreads=0,
+                return_scale=False):
+    """Per-group <W>: array [ninst][nF][Nl//group] (and, with return_scale,
+    the magnitude S of the Richardson sum's terms in the same layout)."""
     loops = _f(loops)
     Nl, ppl = loops.shape[:2]
     cx, cy, T, F = _d(np.atleast_1d(cx)), _d(np.atleast_1d(cy)), _d(np.atleast_1d(T)), \
@@ -188,11 +190,18 @@ def eval_groups(loops, cx, cy, T, F, fld, group=128, fp32=False, nthreads=0):
     n = len(T)
     ng = Nl // group
     out = np.empty((n, len(F), ng))
+    scale = np.empty((n, len(F), ng)) if return_scale else None
     fn = lib().wlo32_eval if fp32 else lib().wlo64_eval
     fn(_ptr(loops, C.c_float), Nl, ppl, n, _ptr(cx, C.c_double), _ptr(cy, C.c_double),
        _ptr(T, C.c_double), len(F), _ptr(F, C.c_double), C.byref(fld), group,
-       _ptr(out, C.c_double), nthreads)
-    return out
+       _ptr(out, C.c_double), _ptr(scale, C.c_double) if return_scale else None, nthreads)
+    return (out, scale) if return_scale else out
+
+
+def werr(w, ref, scale, floor=1e-2):
+    """Error metric of <W> results: |W - W64| / max(|W64|, floor * S), S the
+    magnitude of the Richardson sum's terms (<= 5 for scalar QED)."""
+    return np.max(np.abs(np.asarray(w) - ref) / np.maximum(np.abs(ref), floor * scale))
 
 
 def magfield(rho2, F, fld):

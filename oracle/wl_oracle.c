@@ -151,7 +151,7 @@ double wlo64_evmean(const double *scal, const double *ferm, int n, const int *WL
 static void eval_generic(int fp32, const float *loops, int Nl, int ppl, int ninst,
                          const double *cx, const double *cy, const double *T, int nF,
                          const double *F, const wlo_field *f, int group, double *out,
-                         int nthreads) {
+                         double *scale, int nthreads) {
   const int ng = Nl / group;
 #ifdef _OPENMP
   if (nthreads <= 0) nthreads = omp_get_max_threads();
@@ -162,8 +162,9 @@ static void eval_generic(int fp32, const float *loops, int Nl, int ppl, int nins
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
   for (long task = 0; task < (long)ninst * ng; task++) {
     const int i = (int)(task / ng), g = (int)(task % ng);
-    double acc[16][3];
+    double acc[16][3], aab[16][3];
     memset(acc, 0, sizeof(acc));
+    memset(aab, 0, sizeof(aab));
     const double rtT = sqrt(T[i]);
     for (int l = g * group; l < (g + 1) * group; l++) {
       double gs[3], gf[3];
@@ -182,26 +183,32 @@ static void eval_generic(int fp32, const float *loops, int Nl, int ppl, int nins
         double s[3], fm[3], wv[3];
         finish_loop(gs, gf, T[i], F[j], ppl, s, fm);
         wlo64_wfactors(s, fm, f->fermion, wv);
-        for (int k = 0; k < 3; k++) acc[j][k] += wv[k];
+        for (int k = 0; k < 3; k++) {
+          acc[j][k] += wv[k];
+          aab[j][k] += fabs(wv[k]);
+        }
       }
     }
     for (int j = 0; j < nF && j < 16; j++) {
       double m1 = acc[j][0] / group, m2 = acc[j][1] / group, m4 = acc[j][2] / group;
       out[((size_t)i * nF + j) * ng + g] = 8.0 / 3.0 * m1 - 2.0 * m2 + 1.0 / 3.0 * m4;
+      if (scale)
+        scale[((size_t)i * nF + j) * ng + g] =
+            (8.0 / 3.0 * aab[j][0] + 2.0 * aab[j][1] + 1.0 / 3.0 * aab[j][2]) / group;
     }
   }
 }
 
 void wlo64_eval(const float *loops, int Nl, int ppl, int ninst, const double *cx,
                 const double *cy, const double *T, int nF, const double *F,
-                const wlo_field *f, int group, double *out, int nthreads) {
-  eval_generic(0, loops, Nl, ppl, ninst, cx, cy, T, nF, F, f, group, out, nthreads);
+                const wlo_field *f, int group, double *out, double *scale, int nthreads) {
+  eval_generic(0, loops, Nl, ppl, ninst, cx, cy, T, nF, F, f, group, out, scale, nthreads);
 }
 
 void wlo32_eval(const float *loops, int Nl, int ppl, int ninst, const double *cx,
                 const double *cy, const double *T, int nF, const double *F,
-                const wlo_field *f, int group, double *out, int nthreads) {
-  eval_generic(1, loops, Nl, ppl, ninst, cx, cy, T, nF, F, f, group, out, nthreads);
+                const wlo_field *f, int group, double *out, double *scale, int nthreads) {
+  eval_generic(1, loops, Nl, ppl, ninst, cx, cy, T, nF, F, f, group, out, scale, nthreads);
 }
 
 /* ------------------------------------------------ proper-time integrand -- */
@@ -340,7 +347,7 @@ static void tfunc_groups(double t, const float *loops, int ppl, int ng, double x
     return;
   }
   double cx = xcmx, cy = xcmy, TT = T, FF = F;
-  wlo64_eval(loops, ng * 128, ppl, 1, &cx, &cy, &TT, 1, &FF, f, 128, out, nthreads);
+  wlo64_eval(loops, ng * 128, ppl, 1, &cx, &cy, &TT, 1, &FF, f, 128, out, NULL, nthreads);
   for (int g = 0; g < ng; g++) out[g] = wlo_tfunc_mc(T, out[g], xcmx, xcmy, F, f, q) / t / t;
 }
 

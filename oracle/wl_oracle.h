@@ -88,15 +88,17 @@ double wlo64_evmean(const double *scal, const double *ferm, int n,
 /* ---- many instances: per-group <W> (Richardson-combined).
  * Instances are (cx[i], cy[i], T[i]); all share the field; nF flux values.
  * out[(i*nF + j)*ng + g] = <W> of group g (loops g*G .. g*G+G-1), G = group.
- * nthreads <= 0 uses all OpenMP threads.                                   */
+ * scale (may be NULL), same layout: S = 8/3 <|w_N|> + 2 <|w_N/2|> +
+ * 1/3 <|w_N/4|>, the magnitude of the Richardson sum's terms (the error
+ * scale of the estimator).  nthreads <= 0 uses all OpenMP threads.       */
 void wlo64_eval(const float *loops, int Nl, int ppl, int ninst,
                 const double *cx, const double *cy, const double *T, int nF,
                 const double *F, const wlo_field *f, int group, double *out,
-                int nthreads);
+                double *scale, int nthreads);
 void wlo32_eval(const float *loops, int Nl, int ppl, int ninst,
                 const double *cx, const double *cy, const double *T, int nF,
                 const double *F, const wlo_field *f, int group, double *out,
-                int nthreads);
+                double *scale, int nthreads);
 
 /* ---- proper-time integrand and integral (FP64) ------------------------ */
 typedef struct {

@@ -163,6 +163,32 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
   return WL_OK;
 }
 
+// Double-float per-flux constants of the per-loop epilogue:
+// cph = F h/3 (phase) and csp = F h/3 * fp_scale (spin, times 4T/N per
+// instance on the device), fp_scale being the constant the kernels factor
+// out of f' (Profile<P>::fp_scale).
+template <typename Args>
+void fill_flux(Args &a, const wl_field *f, int nF, const double *F) {
+  const double h3 = 1.0 / (3.0 * (double)f->nint);
+  double fs = 1.0;
+  switch (f->profile) {
+    case WL_PROFILE_SMOOTH: fs = (double)(float)f->lambda2; break;
+    case WL_PROFILE_STEP:
+    case WL_PROFILE_GAUSSIAN: fs = 1.0 / (double)(float)f->lambda2; break;
+    case WL_PROFILE_QUADRATIC: fs = 2.0 / (double)(float)f->lambda2; break;
+    default: fs = 1.0;
+  }
+  for (int j = 0; j < wl::kMaxF; ++j) {
+    const double Fj = j < nF ? F[j] : 0.0;
+    const double cp = Fj * h3, cs = Fj * h3 * fs;
+    a.F[j] = (float)Fj;
+    a.cph_hi[j] = (float)cp;
+    a.cph_lo[j] = (float)(cp - (double)(float)cp);
+    a.csp_hi[j] = (float)cs;
+    a.csp_lo[j] = (float)(cs - (double)(float)cs);
+  }
+}
+
 int lookup(wl_ctx *ctx, int handle, Ensemble *e) {
   auto it = ctx->ens.find(handle);
   if (it == ctx->ens.end()) return fail(ctx, WL_ERR_NOTFOUND, "unknown ensemble %d", handle);
@@ -176,24 +202,30 @@ int set_device(wl_ctx *ctx) {
 }
 
 // stage per-instance constants: cx, cy, rtT = float(sqrt(T)) (intEV.cu:118,
-// 124), tq = 4T/ppl (the 2T/(N/2) spin normalisation, intEV.cu:558-560)
+// 124) and tq = 4T/ppl (the 2T/(N/2) spin normalisation, intEV.cu:558-560)
+// as a float pair hi + lo
 int upload_instances(wl_ctx *ctx, int ninst, const double *cx, const double *cy,
                      const double *T, int ppl) {
   for (int i = 0; i < ninst; ++i) {
     if (!isfinite(cx[i]) || !isfinite(cy[i]) || !(T[i] > 0.0) || !isfinite(T[i]))
       return fail(ctx, WL_ERR_INVALID, "instance %d: need finite centre and T > 0", i);
   }
-  ctx->h_inst.resize((size_t)4 * ninst);
+  const int na = wl::kInstArrays;
+  ctx->h_inst.resize((size_t)na * ninst);
   float *h = ctx->h_inst.data();
   for (int i = 0; i < ninst; ++i) {
+    const double tq = 4.0 * T[i] / (double)ppl;
     h[i] = (float)cx[i];
     h[ninst + i] = (float)cy[i];
     h[2 * ninst + i] = (float)sqrt(T[i]);
-    h[3 * ninst + i] = (float)(4.0 * T[i] / (double)ppl);
+    h[3 * ninst + i] = (float)tq;
+    h[4 * ninst + i] = (float)(tq - (double)(float)tq);
   }
-  WL_CHECK(ctx, ctx->inst.reserve((size_t)4 * ninst));
-  WL_CHECK(ctx, cudaMemcpyAsync(ctx->inst.p, h, sizeof(float) * 4 * ninst,
+  WL_CHECK(ctx, ctx->inst.reserve((size_t)na * ninst));
+  // the staging vector is pageable and reused: copy synchronously
+  WL_CHECK(ctx, cudaMemcpyAsync(ctx->inst.p, h, sizeof(float) * na * ninst,
                                 cudaMemcpyHostToDevice, ctx->stream));
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
   return WL_OK;
 }
 
@@ -459,8 +491,10 @@ static int eval_prologue(wl_ctx *ctx, int handle, const wl_field *field, int nin
 // ctx->inst as [cx | cy | rtT | tq].  Outputs are device pointers (may be
 // NULL).  Returns after enqueueing.
 static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &fd,
-                    bool fermion, int nint, int ninst, int nF, const double *host_F, int group,
+                    const wl_field *field, int ninst, int nF, const double *host_F, int group,
                     double *dg, double *dm, double *ds) {
+  const bool fermion = field->fermion != 0;
+  const int nint = field->nint;
   const bool use_sweep = ninst >= 32;
   int n_chunks, cpg;
   if (use_sweep) {
@@ -489,9 +523,10 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
     a.cx = di;
     a.cy = di + ninst;
     a.rtT = di + 2 * ninst;
-    a.tq = di + 3 * ninst;
+    a.tqh = di + 3 * ninst;
+    a.tql = di + 4 * ninst;
     a.nF = nF;
-    for (int j = 0; j < nF; ++j) a.F[j] = (float)host_F[j];
+    fill_flux(a, field, nF, host_F);
     a.field = fd;
     a.chunk_loops = e.Nl / n_chunks;
     a.n_chunks = n_chunks;
@@ -510,9 +545,10 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
     a.cx = di;
     a.cy = di + ninst;
     a.rtT = di + 2 * ninst;
-    a.tq = di + 3 * ninst;
+    a.tqh = di + 3 * ninst;
+    a.tql = di + 4 * ninst;
     a.nF = nF;
-    for (int j = 0; j < nF; ++j) a.F[j] = (float)host_F[j];
+    fill_flux(a, field, nF, host_F);
     a.field = fd;
     a.partial = ctx->partial.p;
     WL_CHECK(ctx, wl::launch_loopwarp(kprof, fermion, nint, a, ctx->stream));
@@ -542,8 +578,7 @@ int wl_eval(wl_ctx *ctx, int handle, const wl_field *field, int ninst, const dou
     return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu outputs", nout);
   }
   double *dg = ctx->out.p, *dm = dg + (size_t)ninst * nF * ng, *ds = dm + (size_t)ninst * nF;
-  if ((r = run_eval(ctx, e, kprof, fd, field->fermion != 0, field->nint, ninst, nF, host_F,
-                    group, dg, dm, ds)))
+  if ((r = run_eval(ctx, e, kprof, fd, field, ninst, nF, host_F, group, dg, dm, ds)))
     return r;
   ctx->last_launches = 2;
   if (out_group)
@@ -581,11 +616,11 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
     return r;
   if (dev_out_sem && (r = check_device_range(ctx, dev_out_sem, nb * nF, "dev_out_sem")))
     return r;
-  WL_CHECK(ctx, ctx->inst.reserve((size_t)4 * ninst));
+  WL_CHECK(ctx, ctx->inst.reserve((size_t)wl::kInstArrays * ninst));
   WL_CHECK(ctx, wl::launch_instance_setup(dev_cx, dev_cy, dev_T, ninst, e.ppl, ctx->inst.p,
                                           ctx->status.p, ctx->stream));
-  if ((r = run_eval(ctx, e, kprof, fd, field->fermion != 0, field->nint, ninst, nF, host_F,
-                    group, dev_out_group, dev_out_mean, dev_out_sem)))
+  if ((r = run_eval(ctx, e, kprof, fd, field, ninst, nF, host_F, group, dev_out_group,
+                    dev_out_mean, dev_out_sem)))
     return r;
   ctx->last_launches = 3;
   return WL_OK;
@@ -654,9 +689,10 @@ int wl_loops(wl_ctx *ctx, int handle, const wl_field *field, double cx, double c
   a.cx = ctx->inst.p;
   a.cy = ctx->inst.p + 1;
   a.rtT = ctx->inst.p + 2;
-  a.tq = ctx->inst.p + 3;
+  a.tqh = ctx->inst.p + 3;
+  a.tql = ctx->inst.p + 4;
   a.nF = 1;
-  a.F[0] = (float)F;
+  fill_flux(a, field, 1, &F);
   a.field = fd;
   a.partial = ctx->partial.p;
   a.scal = ds;
@@ -773,9 +809,10 @@ double EV(double T, void *p, int *WLlist) {
     a.cx = ctx->inst.p;
     a.cy = ctx->inst.p + 1;
     a.rtT = ctx->inst.p + 2;
-    a.tq = ctx->inst.p + 3;
+    a.tqh = ctx->inst.p + 3;
+    a.tql = ctx->inst.p + 4;
     a.nF = 1;
-    a.F[0] = (float)params.F;
+    fill_flux(a, &f, 1, &params.F);
     a.field = fd;
     a.partial = L.w.p;
     a.scal = params.Wsscal_d;

@@ -278,7 +278,49 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
   sum = t;
 }
 
-// ------------------------------------------------------------ W factors --
+// ------------------------------------------------- double-float (FP32 pairs) --
+// The per-loop phases and spin exponents reach |x| ~ 1e2-1e3; FP32 rounding of
+// their scale factors would shift every loop coherently (relative 1e-7, i.e.
+// 1e-5 in cosh(60)).  The per-loop epilogue therefore works on unevaluated
+// sums hi + lo of two floats (error-free transformations of Knuth / Dekker).
+struct df {
+  float hi, lo;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df df_mul(df x, df y) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+  const df s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, s.lo + x.lo + y.lo);
+}
+__device__ __forceinline__ df df_scale2(df x, float p2) { return {x.hi * p2, x.lo * p2}; }
+
+// cos(x.hi + x.lo): Cody-Waite reduction by 2 pi = C1 + C2 + C3 (Cody and
+// Waite, Software Manual for the Elementary Functions, 1980); C1 = 6.28125
+// has 8 significant bits, so k*C1 is exact for |k| < 2^16 and x.hi - k*C1 is
+// exact by Sterbenz's lemma; then cos(r + e) = cos r - e sin r.
+__device__ __forceinline__ float cos_df(df x) {
+  const float k = rintf(x.hi * 0.15915494f);
+  const float t = fmaf(-k, 6.28125f, x.hi);
+  const float u = fmaf(-k, 1.9353071693331003e-3f, x.lo);
+  df r = two_sum(t, u);
+  r.lo = fmaf(-k, 1.0253131677018246e-11f, r.lo);
+  float sn, cs;
+  sincosf(r.hi, &sn, &cs);
+  return fmaf(-sn, r.lo, cs);
+}
+
 // The reference's sentinel: C abs() of a double truncates to int
 // (Integrand.c:371), so it fires for |x| >= 601; conversions beyond the int
 // range give INT_MIN on x86 (no sentinel), which is mirrored.
@@ -287,57 +329,70 @@ __device__ __forceinline__ bool sentinel600(float x) {
   return ax >= 601.0f && ax < 2147483648.0f;
 }
 
-// cosh in FP64 range: FP32 coshf below |x| = 80, FP64 exp above (FP32 coshf
-// overflows near 89 while the reference's FP64 cosh is finite to 710).
-__device__ __forceinline__ double cosh_wide(float x) {
-  const float ax = fabsf(x);
-  if (ax < 80.0f) return (double)coshf(ax);
-  return 0.5 * exp((double)ax);
+// cosh(x.hi + x.lo) in FP64 range: below |x| = 80 from FP32 exp of the high
+// part, cosh(a + e) = cosh a + e sinh a; above, FP64 exp (FP32 overflows near
+// 89 while the reference's FP64 cosh is finite up to 710).
+__device__ __forceinline__ double cosh_df(df x) {
+  const float a = fabsf(x.hi), e = x.hi < 0.0f ? -x.lo : x.lo;
+  if (a < 80.0f) {
+    const float ex = expf(a), iex = 1.0f / ex;
+    return (double)fmaf(0.5f * (ex - iex), e, 0.5f * (ex + iex));
+  }
+  return 0.5 * exp((double)a + (double)e);
 }
 
-// Per-loop factors of EVMean (Integrand.c:352-390):
-//   w0 = W_N   = cos(phi_x/2 + (phi_y+phi_z)/4) [* cosh(same of psi)]
-//   w1 = W_N/2 = cos(phi_x)                      [* cosh(psi_x)]
-//   w2 = W_N/4 = cos((phi_y+phi_z)/2)            [* cosh(same of psi)]
+// Per-loop factors of EVMean (Integrand.c:352-390) from the sub-loop phases
+// p[k] and spin exponents q[k] (k: N/2, N/4b, N/4a):
+//   w0 = W_N   = cos(p0/2 + (p1+p2)/4) [* cosh(same of q)]
+//   w1 = W_N/2 = cos(p0)                [* cosh(q0)]
+//   w2 = W_N/4 = cos((p1+p2)/2)         [* cosh(same of q)]
+// with the reference's 1e10 sentinel when a spin exponent truncates above 600.
 template <bool FERM>
-__device__ __forceinline__ void wfactors(float p0, float p1, float p2, float q0, float q1,
-                                         float q2, double &w0, double &w1, double &w2) {
-  const float nb4 = p1 + p2;
-  w0 = (double)cosf(fmaf(0.5f, p0, 0.25f * nb4));
-  w1 = (double)cosf(p0);
-  w2 = (double)cosf(0.5f * nb4);
+__device__ __forceinline__ void wfactors(const df p[3], const df q[3], double &w0, double &w1,
+                                         double &w2) {
+  const df nb4 = df_add(p[1], p[2]);
+  w0 = (double)cos_df(df_add(df_scale2(p[0], 0.5f), df_scale2(nb4, 0.25f)));
+  w1 = (double)cos_df(p[0]);
+  w2 = (double)cos_df(df_scale2(nb4, 0.5f));
   if (FERM) {
-    const float nb4f = q1 + q2;
-    if (sentinel600(nb4f) || sentinel600(q0)) {
+    const df nb4f = df_add(q[1], q[2]);
+    if (sentinel600(nb4f.hi) || sentinel600(q[0].hi)) {
       w0 *= 1.0e10;
       w1 *= 1.0e10;
       w2 *= 1.0e10;
     } else {
-      w0 *= cosh_wide(fmaf(0.5f, q0, 0.25f * nb4f));
-      w1 *= cosh_wide(q0);
-      w2 *= cosh_wide(0.5f * nb4f);
+      w0 *= cosh_df(df_add(df_scale2(q[0], 0.5f), df_scale2(nb4f, 0.25f)));
+      w1 *= cosh_df(q[0]);
+      w2 *= cosh_df(df_scale2(nb4f, 0.5f));
     }
   }
 }
 
-// Finishes one loop at one instance (intEV.cu:553-561 and the EVMean
-// factors): G*, H* are the loop's Simpson sums without the h/3 factor and
-// the f' scale; phases are F*G*h/3 and spin exponents 2F T sum/(N/2) resp.
-// 2F T sum/(N/4) (tq = 4T/N).  The W factors of every flux value are added
-// to acc in FP64.
-template <int P, bool FERM>
-__device__ __forceinline__ void loop_epilogue(const float G[3], const float H[3],
-                                              const FieldDev &F, float h3, float tq, int nF,
-                                              const float *Fv, double (&acc)[kMaxF][3]) {
-  const float fs = Profile<P>::fp_scale(F) * h3;
-  const float g0 = G[0] * h3, g1 = G[1] * h3, g2 = G[2] * h3;
-  const float s0 = H[0] * fs * tq, s1 = H[1] * fs * (2.0f * tq), s2 = H[2] * fs * (2.0f * tq);
+// Finishes one loop at one instance (intEV.cu:553-561 with the EVMean
+// factors).  G[k], H[k]: the loop's Simpson sums of xyyx f/rho^2 and of f'
+// (without h/3 and the f' scale).  cph[j] = F_j h/3 and csp[j] = F_j h/3 *
+// fp_scale * 4T/N (per instance) are double-float constants, so the phase is
+// F G h/3 and the spin exponent 2 F T sum/(N/2) (N/2 loop) or
+// 2 F T sum/(N/4) (N/4 loops).  The W factors are added to acc in FP64.
+template <bool FERM>
+__device__ __forceinline__ void loop_epilogue(const df G[3], const df H[3], const df *cph,
+                                              const df *csp, int nF,
+                                              double (&acc)[kMaxF][3]) {
 #pragma unroll
   for (int j = 0; j < kMaxF; ++j) {
     if (j < nF) {
-      const float f = Fv[j];
+      df p[3], q[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) p[k] = df_mul(cph[j], G[k]);
+      if (FERM) {
+        q[0] = df_mul(csp[j], H[0]);
+        q[1] = df_scale2(df_mul(csp[j], H[1]), 2.0f);
+        q[2] = df_scale2(df_mul(csp[j], H[2]), 2.0f);
+      } else {
+        q[0] = q[1] = q[2] = df{0.0f, 0.0f};
+      }
       double w0, w1, w2;
-      wfactors<FERM>(f * g0, f * g1, f * g2, f * s0, f * s1, f * s2, w0, w1, w2);
+      wfactors<FERM>(p, q, w0, w1, w2);
       acc[j][0] += w0;
       acc[j][1] += w1;
       acc[j][2] += w2;

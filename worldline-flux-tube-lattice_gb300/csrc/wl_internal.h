@@ -25,9 +25,11 @@ struct SweepArgs {
   int ninst;
   const float *cx, *cy;  // [ninst] centre of mass
   const float *rtT;      // [ninst] float(sqrt(T)) as the reference passes it
-  const float *tq;       // [ninst] 4 T / ppl: spin normalisation 2T/(N/2)
+  const float *tqh, *tql;  // [ninst] 4 T / ppl (spin normalisation 2T/(N/2)), hi + lo
   int nF;
   float F[kMaxF];
+  // double-float per-flux constants: cph = F h/3, csp = F h/3 fp_scale
+  float cph_hi[kMaxF], cph_lo[kMaxF], csp_hi[kMaxF], csp_lo[kMaxF];
   FieldDev field;
   int chunk_loops;   // loops per CTA
   int n_chunks;      // Nl / chunk_loops
@@ -44,9 +46,10 @@ struct LoopArgs {
   const float4 *loops;
   int Nl, ppl;
   int ninst;
-  const float *cx, *cy, *rtT, *tq;
+  const float *cx, *cy, *rtT, *tqh, *tql;
   int nF;
   float F[kMaxF];
+  float cph_hi[kMaxF], cph_lo[kMaxF], csp_hi[kMaxF], csp_lo[kMaxF];
   FieldDev field;
   double *partial;  // [Nl][nF][3][ninst]  (chunk = one loop)
   float4 *scal;     // optional [ninst][Nl] Wsscal of F[0]
@@ -70,7 +73,7 @@ cudaError_t launch_list_mean(const double *partial, const int *list, int n, doub
                              cudaStream_t s);
 
 // device-resident instances (cx, cy, T) -> the sweep's float arrays
-// [cx | cy | rtT | tq]; flags T <= 0 or non-finite values in *status
+// [cx | cy | rtT | tq_hi | tq_lo]; flags T <= 0 or non-finite values in *status
 cudaError_t launch_instance_setup(const double *cx, const double *cy, const double *T,
                                   int ninst, int ppl, float *out, int *status,
                                   cudaStream_t s);
@@ -85,6 +88,8 @@ cudaError_t launch_vloops(uint64_t seed, int first, int Nl, int ppl, float4 *out
                           cudaStream_t s);
 
 // bytes of dynamic shared memory of the sweep kernel
+constexpr int kInstArrays = 5;  // cx, cy, rtT, tq_hi, tq_lo
+
 constexpr size_t sweep_smem_bytes() {
   return (size_t)kSweepStages * kSweepChunkPts * sizeof(float4);
 }

@@ -128,7 +128,7 @@ cudaError_t launch_list_mean(const double *partial, const int *list, int n, doub
 }
 
 // instance set-up on the device: the same float conversions as the host path
-// (rtT = float(sqrt(T)), tq = float(4T/ppl))
+// (rtT = float(sqrt(T)), tq = 4T/ppl as a float pair hi + lo)
 __global__ void instance_setup_kernel(const double *__restrict__ cx,
                                       const double *__restrict__ cy,
                                       const double *__restrict__ T, int ninst, int ppl,
@@ -141,8 +141,10 @@ __global__ void instance_setup_kernel(const double *__restrict__ cx,
   const double tt = ok ? t : 1.0;
   out[i] = ok ? (float)x : 0.0f;
   out[ninst + i] = ok ? (float)y : 0.0f;
+  const double tq = 4.0 * tt / (double)ppl;
   out[2 * ninst + i] = (float)sqrt(tt);
-  out[3 * ninst + i] = (float)(4.0 * tt / (double)ppl);
+  out[3 * ninst + i] = (float)tq;
+  out[4 * ninst + i] = (float)(tq - (double)(float)tq);
 }
 
 cudaError_t launch_instance_setup(const double *cx, const double *cy, const double *T,

@@ -40,9 +40,17 @@ __global__ void __launch_bounds__(kSweepThreads)
   const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
   const int K = A.chunk_loops * nck;
 
-  const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic], tq = A.tq[ic];
+  const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic];
   const FieldDev &F = A.field;
-  const float h3 = (NINT > 0 ? 1.0f / (float)NINT : F.h) * (1.0f / 3.0f);
+  df cph[kMaxF], csp[kMaxF];
+  {
+    const df tq = {A.tqh[ic], A.tql[ic]};
+#pragma unroll
+    for (int j = 0; j < kMaxF; ++j) {
+      cph[j] = df{A.cph_hi[j], A.cph_lo[j]};
+      csp[j] = df_mul(df{A.csp_hi[j], A.csp_lo[j]}, tq);
+    }
+  }
 
   if (tid == 0) {
     for (int st = 0; st < kSweepStages; ++st) mbar_init(&full_bar[st], 1);
@@ -152,9 +160,11 @@ __global__ void __launch_bounds__(kSweepThreads)
       kahan_add(sp[0], sc[0], ts0);
       kahan_add(sp[1], sc[1], ts1);
       kahan_add(sp[2], sc[2], ts2);
-      const float G[3] = {ph[0] - pc[0], ph[1] - pc[1], ph[2] - pc[2]};
-      const float H[3] = {sp[0] - sc[0], sp[1] - sc[1], sp[2] - sc[2]};
-      loop_epilogue<P, FERM>(G, H, F, h3, tq, A.nF, A.F, acc);
+      const df G[3] = {fast_two_sum(ph[0], -pc[0]), fast_two_sum(ph[1], -pc[1]),
+                       fast_two_sum(ph[2], -pc[2])};
+      const df H[3] = {fast_two_sum(sp[0], -sc[0]), fast_two_sum(sp[1], -sc[1]),
+                       fast_two_sum(sp[2], -sc[2])};
+      loop_epilogue<FERM>(G, H, cph, csp, A.nF, acc);
     }
 
     __syncthreads();  // every thread is done with stage st
@@ -192,7 +202,7 @@ __global__ void __launch_bounds__(kLoopWarps * 32)
   const int l = blockIdx.x * kLoopWarps + (threadIdx.x >> 5);
   const int inst = blockIdx.y;
   if (l >= A.Nl) return;  // whole warp
-  const float cx = A.cx[inst], cy = A.cy[inst], s = A.rtT[inst], tq = A.tq[inst];
+  const float cx = A.cx[inst], cy = A.cy[inst], s = A.rtT[inst];
   const FieldDev &F = A.field;
   const float2 *w = reinterpret_cast<const float2 *>(A.loops + (size_t)l * A.ppl);
   auto pt = [&](int p, float &x, float &y) {
@@ -228,25 +238,35 @@ __global__ void __launch_bounds__(kLoopWarps * 32)
     }
   }
   if (lane == 0) {
-    const float h3 = (NINT > 0 ? 1.0f / (float)NINT : F.h) * (1.0f / 3.0f);
+    const df tq = {A.tqh[inst], A.tql[inst]};
+    df cph[kMaxF], csp[kMaxF];
+#pragma unroll
+    for (int j = 0; j < kMaxF; ++j) {
+      cph[j] = df{A.cph_hi[j], A.cph_lo[j]};
+      csp[j] = df_mul(df{A.csp_hi[j], A.csp_lo[j]}, tq);
+    }
+    const df G[3] = {df{ph[0], 0.f}, df{ph[1], 0.f}, df{ph[2], 0.f}};
+    const df H[3] = {df{sp[0], 0.f}, df{sp[1], 0.f}, df{sp[2], 0.f}};
     double acc[kMaxF][3];
 #pragma unroll
     for (int j = 0; j < kMaxF; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0;
-    loop_epilogue<P, FERM>(ph, sp, F, h3, tq, A.nF, A.F, acc);
+    loop_epilogue<FERM>(G, H, cph, csp, A.nF, acc);
 #pragma unroll
     for (int j = 0; j < kMaxF; ++j)
       if (j < A.nF)
 #pragma unroll
         for (int r = 0; r < 3; ++r)
           A.partial[((size_t)(l * A.nF + j) * 3 + r) * A.ninst + inst] = acc[j][r];
+    // Wsscal / Wsferm of the first flux value (intEV.cu:553-561)
     const size_t o = (size_t)inst * A.Nl + l;
-    if (A.scal) A.scal[o] = make_float4(A.F[0] * ph[0] * h3, A.F[0] * ph[1] * h3,
-                                        A.F[0] * ph[2] * h3, 0.0f);
-    if (FERM && A.ferm) {
-      const float fs = Profile<P>::fp_scale(F) * h3 * A.F[0];
-      A.ferm[o] = make_float4(sp[0] * fs * tq, sp[1] * fs * 2.0f * tq,
-                              sp[2] * fs * 2.0f * tq, 0.0f);
-    }
+    auto val = [](df x) { return x.hi + x.lo; };
+    if (A.scal)
+      A.scal[o] = make_float4(val(df_mul(cph[0], G[0])), val(df_mul(cph[0], G[1])),
+                              val(df_mul(cph[0], G[2])), 0.0f);
+    if (FERM && A.ferm)
+      A.ferm[o] = make_float4(val(df_mul(csp[0], H[0])),
+                              2.0f * val(df_mul(csp[0], H[1])),
+                              2.0f * val(df_mul(csp[0], H[2])), 0.0f);
   }
 }
 
