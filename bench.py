@@ -56,11 +56,14 @@ ALG_MUFU_PER_SEG = 5
 ALG_BYTES_PER_POINT = 16
 
 
-def workload():
-    T = np.geomspace(1e-3, 1e3, NT)
-    rho = np.linspace(0.0, 8.0, NRHO)
-    cx = np.repeat(rho, NT)
-    T = np.tile(T, NRHO)
+def workload(small=False):
+    """(cx, cy, T) of every instance; small: 8 T x 16 rho of the same ranges
+    (the profiling case: one instance tile, same ensemble)."""
+    nt, nrho = (8, 16) if small else (NT, NRHO)
+    T = np.geomspace(1e-3, 1e3, nt)
+    rho = np.linspace(0.0, 8.0, nrho)
+    cx = np.repeat(rho, nt)
+    T = np.tile(T, nrho)
     cy = np.zeros_like(cx)
     return cx, cy, T
 
@@ -207,6 +210,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: 128 instances on the full ensemble, no e2e/cpu")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -221,8 +226,10 @@ def main():
     torch.cuda.set_device(local)
     ctx = wltube.Context(local)
     fld = wltube.field("smooth", fermion=1, nint=NINT)
-    cx, cy, T = workload()
+    cx, cy, T = workload(args.small)
     ninst = len(T)
+    if args.small:
+        args.no_e2e = args.no_cpu = True
     h = ctx.generate(SEED, NL, PPL)
     dcx = torch.tensor(cx, dtype=torch.float64, device="cuda")
     dcy = torch.tensor(cy, dtype=torch.float64, device="cuda")

@@ -202,8 +202,9 @@ int set_device(wl_ctx *ctx) {
 }
 
 // stage per-instance constants: cx, cy, rtT = float(sqrt(T)) (intEV.cu:118,
-// 124) and tq = 4T/ppl (the 2T/(N/2) spin normalisation, intEV.cu:558-560)
-// as a float pair hi + lo
+// 124) and tq = 4 rtT^2/ppl (the 2T/(N/2) spin normalisation,
+// intEV.cu:558-560) as a float pair hi + lo.  The kernel thus evaluates the
+// instance (float(cx), float(cy), T' = float(sqrt(T))^2) exactly.
 int upload_instances(wl_ctx *ctx, int ninst, const double *cx, const double *cy,
                      const double *T, int ppl) {
   for (int i = 0; i < ninst; ++i) {
@@ -214,10 +215,13 @@ int upload_instances(wl_ctx *ctx, int ninst, const double *cx, const double *cy,
   ctx->h_inst.resize((size_t)na * ninst);
   float *h = ctx->h_inst.data();
   for (int i = 0; i < ninst; ++i) {
-    const double tq = 4.0 * T[i] / (double)ppl;
+    // the loops are scaled by float(sqrt(T)); the spin normalisation uses the
+    // same T' = rtT^2, as the reference's rtT*rtT (intEV.cu:558)
+    const float rtT = (float)sqrt(T[i]);
+    const double tq = 4.0 * ((double)rtT * (double)rtT) / (double)ppl;
     h[i] = (float)cx[i];
     h[ninst + i] = (float)cy[i];
-    h[2 * ninst + i] = (float)sqrt(T[i]);
+    h[2 * ninst + i] = rtT;
     h[3 * ninst + i] = (float)tq;
     h[4 * ninst + i] = (float)(tq - (double)(float)tq);
   }
@@ -229,14 +233,13 @@ int upload_instances(wl_ctx *ctx, int ninst, const double *cx, const double *cy,
   return WL_OK;
 }
 
-// loops per CTA of the instance-parallel sweep: a divisor of the group size,
-// halved until the grid has at least ~12 CTAs per SM (load balance)
-int plan_chunk(wl_ctx *ctx, int ninst, int Nl, int group) {
-  const long tiles = (ninst + wl::kSweepThreads - 1) / wl::kSweepThreads;
-  int lc = group;
-  while (lc % 2 == 0 && lc > 1 && tiles * (long)(Nl / lc) < 12L * ctx->num_sms &&
-         Nl / (lc / 2) <= 65535)
-    lc /= 2;
+// Loops per CTA of the instance-parallel sweep: the largest divisor of the
+// group size not above 8.  It depends on the ensemble's grouping only, never on
+// the batch, so an instance's partial sums -- and its result, bit for bit --
+// are the same whatever other instances share the launch.
+int plan_chunk(int group) {
+  int lc = 8;
+  while (group % lc) lc /= 2;
   return lc;
 }
 
@@ -498,7 +501,7 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
   const bool use_sweep = ninst >= 32;
   int n_chunks, cpg;
   if (use_sweep) {
-    const int lc = plan_chunk(ctx, ninst, e.Nl, group);
+    const int lc = plan_chunk(group);
     n_chunks = e.Nl / lc;
     if (n_chunks > 65535)
       return fail(ctx, WL_ERR_INVALID, "group %d too small for Nl = %d (grid limit)", group, e.Nl);

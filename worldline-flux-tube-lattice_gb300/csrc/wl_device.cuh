@@ -108,9 +108,11 @@ struct Profile;
 
 template <>
 struct Profile<kSmooth> {  // f = r2/(l2+r2): f/r2 = 1/(l2+r2), f' = l2 (f/r2)^2
-  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
-                                              float &fp) {
-    g = rcp_fast(F.l2 + r2);
+  // evaluated on d = l2 + r2: the segment folds l2 into the constant term of
+  // its rho^2 polynomial once instead of adding it at every node
+  static __device__ __forceinline__ float shift(const FieldDev &F) { return F.l2; }
+  static __device__ __forceinline__ void eval(float d, const FieldDev &, float &g, float &fp) {
+    g = rcp_fast(d);
     fp = g * g;
   }
   static __device__ __forceinline__ float fp_scale(const FieldDev &F) { return F.l2; }
@@ -220,6 +222,16 @@ struct Profile<kFixflux> : FixfluxProfile<false> {};
 template <>
 struct Profile<kFixfluxFF> : FixfluxProfile<true> {};
 
+// rho^2 shift folded into the segment polynomial (Profile<P>::shift where a
+// profile evaluates on l2 + rho^2, else 0)
+template <int P>
+__device__ __forceinline__ float profile_shift(const FieldDev &F) {
+  if constexpr (P == kSmooth)
+    return Profile<P>::shift(F);
+  else
+    return 0.0f;
+}
+
 // ------------------------------------------------------------- segment --
 // One segment z_i -> z_j of a sub-loop (intEV.cu:526-552 with Idt,
 // intEV.cu:408-459): rho^2(t) = a + 2bt + ct^2 with a = |z_i|^2,
@@ -239,13 +251,21 @@ __device__ __forceinline__ void segment(float zix, float ziy, float zjx, float z
   b = fmaxf(b, F.clampB);
   c = fmaxf(c, F.clampC);
   const float b2 = b + b;
-  const float ae = fmaxf(a + b2 + c, F.clampE);
+  // The end-value and interior floors (1e-8, 1e-10 in the reference) can only
+  // act on the dividing (lattice) profiles: with a, b, c clamped positive,
+  // rho^2(t) = a + 2bt + ct^2 >= a >= 1e-8 for t in [0, 1], and the closed
+  // forms of the other profiles are finite at rho^2 -> 0 in exact mode.
+  constexpr bool kFloor = Profile<P>::kHeavy;
+  const float as = a + profile_shift<P>(F);
+  float ae = (as + b2) + c;
+  if (kFloor) ae = fmaxf(ae, F.clampE);
   float g0, f0, g1, f1;
-  Profile<P>::eval(a, F, g0, f0);
+  Profile<P>::eval(as, F, g0, f0);
   Profile<P>::eval(ae, F, g1, f1);
   float so = 0.0f, se = 0.0f, fo = 0.0f, fe = 0.0f;
   auto node = [&](int j, float t) {
-    const float r2 = fmaxf(fmaf(fmaf(c, t, b2), t, a), F.clampI);
+    float r2 = fmaf(fmaf(c, t, b2), t, as);
+    if (kFloor) r2 = fmaxf(r2, F.clampI);
     float g, fp;
     Profile<P>::eval(r2, F, g, fp);
     if (j & 1) {

@@ -128,7 +128,7 @@ cudaError_t launch_list_mean(const double *partial, const int *list, int n, doub
 }
 
 // instance set-up on the device: the same float conversions as the host path
-// (rtT = float(sqrt(T)), tq = 4T/ppl as a float pair hi + lo)
+// (rtT = float(sqrt(T)), tq = 4 rtT^2/ppl as a float pair hi + lo)
 __global__ void instance_setup_kernel(const double *__restrict__ cx,
                                       const double *__restrict__ cy,
                                       const double *__restrict__ T, int ninst, int ppl,
@@ -141,8 +141,9 @@ __global__ void instance_setup_kernel(const double *__restrict__ cx,
   const double tt = ok ? t : 1.0;
   out[i] = ok ? (float)x : 0.0f;
   out[ninst + i] = ok ? (float)y : 0.0f;
-  const double tq = 4.0 * tt / (double)ppl;
-  out[2 * ninst + i] = (float)sqrt(tt);
+  const float rtT = (float)sqrt(tt);
+  const double tq = 4.0 * ((double)rtT * (double)rtT) / (double)ppl;
+  out[2 * ninst + i] = rtT;
   out[3 * ninst + i] = (float)tq;
   out[4 * ninst + i] = (float)(tq - (double)(float)tq);
 }
@@ -180,7 +181,8 @@ __global__ void peak_rcp_kernel(int iters, float *sink) {
   for (int k = 0; k < 8; ++k) a[k] = 1.5f + 1e-3f * (float)(threadIdx.x + k);
   for (int i = 0; i < iters; ++i) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = rcp_fast(a[k]);
+    for (int k = 0; k < 8; ++k)  // volatile: rcp(rcp(x)) must not be folded
+      asm volatile("rcp.approx.ftz.f32 %0, %1;" : "=f"(a[k]) : "f"(a[k]));
   }
   float s = 0.f;
 #pragma unroll

@@ -53,8 +53,11 @@ class Float4(C.Structure):
 
 
 class Wparams(C.Structure):
-    """struct Wparams of wl_legacy.h (the reference's intT.h)."""
+    """struct Wparams of wl_legacy.h (the reference's intT.h).  CUDA's float4
+    is 16-byte aligned, so xcm sits at offset 32 and the struct is 128 bytes;
+    ctypes has no alignment attribute, hence the explicit padding."""
     _fields_ = [("Nl", C.c_int), ("Nppl", C.c_int), ("F", C.c_double), ("l2", C.c_double),
+                ("_pad_xcm", C.c_char * 8),
                 ("xcm", Float4), ("Wsscal_h", C.c_void_p), ("Wsscal_d", C.c_void_p),
                 ("Wsferm_h", C.c_void_p), ("Wsferm_d", C.c_void_p),
                 ("worldlines", C.c_void_p), ("SE", C.c_double), ("nBlocks", C.c_int),
