@@ -390,32 +390,33 @@ __device__ __forceinline__ void wfactors(const df p[3], const df q[3], double &w
 
 // Finishes one loop at one instance (intEV.cu:553-561 with the EVMean
 // factors).  G[k], H[k]: the loop's Simpson sums of xyyx f/rho^2 and of f'
-// (without h/3 and the f' scale).  cph[j] = F_j h/3 and csp[j] = F_j h/3 *
-// fp_scale * 4T/N (per instance) are double-float constants, so the phase is
-// F G h/3 and the spin exponent 2 F T sum/(N/2) (N/2 loop) or
-// 2 F T sum/(N/4) (N/4 loops).  The W factors are added to acc in FP64.
-template <bool FERM>
-__device__ __forceinline__ void loop_epilogue(const df G[3], const df H[3], const df *cph,
-                                              const df *csp, int nF,
-                                              double (&acc)[kMaxF][3]) {
+// (without h/3 and the f' scale).  Per flux value j, cph_j = F_j h/3 and
+// csp_j = F_j h/3 fp_scale are double-float constants and tq = 4T/N is the
+// instance's, so the phase is F G h/3 and the spin exponent 2 F T sum/(N/2)
+// (N/2 loop) or 2 F T sum/(N/4) (N/4 loops).  add(j, w0, w1, w2) receives the
+// W factors (accumulated in FP64 by the caller).
+template <bool FERM, class Add>
+__device__ __forceinline__ void loop_epilogue(const df G[3], const df H[3], const float *cph_hi,
+                                              const float *cph_lo, const float *csp_hi,
+                                              const float *csp_lo, df tq, int nF, Add &&add) {
 #pragma unroll
   for (int j = 0; j < kMaxF; ++j) {
     if (j < nF) {
+      const df cph = {cph_hi[j], cph_lo[j]};
       df p[3], q[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) p[k] = df_mul(cph[j], G[k]);
+      for (int k = 0; k < 3; ++k) p[k] = df_mul(cph, G[k]);
       if (FERM) {
-        q[0] = df_mul(csp[j], H[0]);
-        q[1] = df_scale2(df_mul(csp[j], H[1]), 2.0f);
-        q[2] = df_scale2(df_mul(csp[j], H[2]), 2.0f);
+        const df csp = df_mul(df{csp_hi[j], csp_lo[j]}, tq);
+        q[0] = df_mul(csp, H[0]);
+        q[1] = df_scale2(df_mul(csp, H[1]), 2.0f);
+        q[2] = df_scale2(df_mul(csp, H[2]), 2.0f);
       } else {
         q[0] = q[1] = q[2] = df{0.0f, 0.0f};
       }
       double w0, w1, w2;
       wfactors<FERM>(p, q, w0, w1, w2);
-      acc[j][0] += w0;
-      acc[j][1] += w1;
-      acc[j][2] += w2;
+      add(j, w0, w1, w2);
     }
   }
 }

@@ -16,6 +16,12 @@ enum : int { kDevOk = 0, kDevTimeout = 1, kDevBadInstance = 2 };
 // (instance tile, chunk of loops); the chunk's loops are streamed through a
 // shared-memory ring by bulk copies and every thread walks every point.
 constexpr int kSweepThreads = 128;   // instances per CTA
+// resident CTAs per SM the light-profile sweep is compiled for (register cap
+// 65536 / (128 * blocks)); the lattice profiles use 4
+#ifndef WL_SWEEP_MIN_BLOCKS
+#define WL_SWEEP_MIN_BLOCKS 6
+#endif
+constexpr int kSweepMinBlocks = WL_SWEEP_MIN_BLOCKS;
 constexpr int kSweepStages = 4;      // shared-memory ring depth
 constexpr int kSweepChunkPts = 256;  // points per bulk copy (4 KiB)
 

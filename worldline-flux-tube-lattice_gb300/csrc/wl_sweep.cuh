@@ -26,11 +26,14 @@
 namespace wl {
 
 template <int P, bool FERM, int NINT>
-__global__ void __launch_bounds__(kSweepThreads)
+__global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweepMinBlocks)
     sweep_kernel(const __grid_constant__ SweepArgs A) {
   extern __shared__ __align__(128) float4 ring[];  // [kSweepStages][kSweepChunkPts]
   __shared__ __align__(8) uint64_t full_bar[kSweepStages];
   __shared__ int sm_bad;
+  // FP64 W-factor sums per (flux value, factor, instance): kept in shared
+  // memory (touched once per loop) so they do not hold 24 registers
+  __shared__ double sacc[kMaxF * 3][kSweepThreads];
 
   const int tid = threadIdx.x;
   const int inst = blockIdx.x * kSweepThreads + tid;
@@ -42,15 +45,7 @@ __global__ void __launch_bounds__(kSweepThreads)
 
   const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic];
   const FieldDev &F = A.field;
-  df cph[kMaxF], csp[kMaxF];
-  {
-    const df tq = {A.tqh[ic], A.tql[ic]};
-#pragma unroll
-    for (int j = 0; j < kMaxF; ++j) {
-      cph[j] = df{A.cph_hi[j], A.cph_lo[j]};
-      csp[j] = df_mul(df{A.csp_hi[j], A.csp_lo[j]}, tq);
-    }
-  }
+  const df tq = {A.tqh[ic], A.tql[ic]};
 
   if (tid == 0) {
     for (int st = 0; st < kSweepStages; ++st) mbar_init(&full_bar[st], 1);
@@ -72,9 +67,8 @@ __global__ void __launch_bounds__(kSweepThreads)
   if (tid == 0)
     for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
 
-  double acc[kMaxF][3];
 #pragma unroll
-  for (int j = 0; j < kMaxF; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0;
+  for (int r = 0; r < kMaxF * 3; ++r) sacc[r][tid] = 0.0;
 
   // running sums of the current loop: phase and spin, each with compensation
   float ph[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
@@ -164,7 +158,12 @@ __global__ void __launch_bounds__(kSweepThreads)
                        fast_two_sum(ph[2], -pc[2])};
       const df H[3] = {fast_two_sum(sp[0], -sc[0]), fast_two_sum(sp[1], -sc[1]),
                        fast_two_sum(sp[2], -sc[2])};
-      loop_epilogue<FERM>(G, H, cph, csp, A.nF, acc);
+      loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
+                          [&](int j, double w0, double w1, double w2) {
+                            sacc[3 * j][tid] += w0;
+                            sacc[3 * j + 1][tid] += w1;
+                            sacc[3 * j + 2][tid] += w2;
+                          });
     }
 
     __syncthreads();  // every thread is done with stage st
@@ -186,12 +185,8 @@ __global__ void __launch_bounds__(kSweepThreads)
   }
 
   if (inst < A.ninst) {
-#pragma unroll
-    for (int j = 0; j < kMaxF; ++j)
-      if (j < A.nF)
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-          A.partial[((size_t)(chunk * A.nF + j) * 3 + r) * A.ninst + inst] = acc[j][r];
+    for (int r = 0; r < A.nF * 3; ++r)
+      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + inst] = sacc[r][tid];
   }
 }
 
@@ -239,34 +234,27 @@ __global__ void __launch_bounds__(kLoopWarps * 32)
   }
   if (lane == 0) {
     const df tq = {A.tqh[inst], A.tql[inst]};
-    df cph[kMaxF], csp[kMaxF];
-#pragma unroll
-    for (int j = 0; j < kMaxF; ++j) {
-      cph[j] = df{A.cph_hi[j], A.cph_lo[j]};
-      csp[j] = df_mul(df{A.csp_hi[j], A.csp_lo[j]}, tq);
-    }
     const df G[3] = {df{ph[0], 0.f}, df{ph[1], 0.f}, df{ph[2], 0.f}};
     const df H[3] = {df{sp[0], 0.f}, df{sp[1], 0.f}, df{sp[2], 0.f}};
-    double acc[kMaxF][3];
-#pragma unroll
-    for (int j = 0; j < kMaxF; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0;
-    loop_epilogue<FERM>(G, H, cph, csp, A.nF, acc);
-#pragma unroll
-    for (int j = 0; j < kMaxF; ++j)
-      if (j < A.nF)
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-          A.partial[((size_t)(l * A.nF + j) * 3 + r) * A.ninst + inst] = acc[j][r];
+    loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
+                        [&](int j, double w0, double w1, double w2) {
+                          double *o = A.partial + ((size_t)(l * A.nF + j) * 3) * A.ninst + inst;
+                          o[0] = w0;
+                          o[A.ninst] = w1;
+                          o[2 * (size_t)A.ninst] = w2;
+                        });
     // Wsscal / Wsferm of the first flux value (intEV.cu:553-561)
     const size_t o = (size_t)inst * A.Nl + l;
     auto val = [](df x) { return x.hi + x.lo; };
+    const df cph0 = {A.cph_hi[0], A.cph_lo[0]};
     if (A.scal)
-      A.scal[o] = make_float4(val(df_mul(cph[0], G[0])), val(df_mul(cph[0], G[1])),
-                              val(df_mul(cph[0], G[2])), 0.0f);
-    if (FERM && A.ferm)
-      A.ferm[o] = make_float4(val(df_mul(csp[0], H[0])),
-                              2.0f * val(df_mul(csp[0], H[1])),
-                              2.0f * val(df_mul(csp[0], H[2])), 0.0f);
+      A.scal[o] = make_float4(val(df_mul(cph0, G[0])), val(df_mul(cph0, G[1])),
+                              val(df_mul(cph0, G[2])), 0.0f);
+    if (FERM && A.ferm) {
+      const df csp0 = df_mul(df{A.csp_hi[0], A.csp_lo[0]}, tq);
+      A.ferm[o] = make_float4(val(df_mul(csp0, H[0])), 2.0f * val(df_mul(csp0, H[1])),
+                              2.0f * val(df_mul(csp0, H[2])), 0.0f);
+    }
   }
 }
 
