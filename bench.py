@@ -46,11 +46,12 @@ NT, NRHO = 128, 64
 FLUX = [0.1, 1.0, 10.0]
 NINT = 4
 GROUP = 128
-# FP32 and MUFU operations per loop-segment of the smooth spinor kernel at 5
-# nodes, counted from the source (segment() in csrc/wl_device.cuh): point
-# transform 2, setup 8, clamps 3, end value 4, 3 interior rho^2 x 3, 5 nodes
-# x (add + square), Simpson sums 6 + 8 combines -> 52 FP32; 5 reciprocals.
-ALG_FP32_PER_SEG = 52
+# Algorithmic FP32 and MUFU operations per loop-segment of smooth spinor QED
+# at 5 Simpson nodes (fixed, not tuned): segment set-up ~25 FP32 (scale and
+# shift 4, a/b/c 6, cross term 2, clamps 4, Simpson combine 3, compensated
+# sums 8); per node 4 FP32 + 1 MUFU reciprocal (f/rho^2 = 1/(l2 + rho^2)) and
+# 2 FP32 for the spin part: 25 + 5 x 6 = 55 FP32, 5 MUFU.
+ALG_FP32_PER_SEG = 55
 ALG_MUFU_PER_SEG = 5
 # loop data a segment reads (one float4 point) -- HBM side of the roofline
 ALG_BYTES_PER_POINT = 16
