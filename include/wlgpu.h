@@ -125,6 +125,31 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
  * lane operations per second over the whole device (about 0.1 s of work). */
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s);
 
+/* Allocation-free variant of wl_eval_device.  No counterpart in the
+ * reference.  For callers that cannot let a library allocate device memory:
+ * a framework whose caching allocator owns the whole device (a cudaMalloc
+ * behind its back can fail or break its accounting), code where cudaMalloc is
+ * not permitted, or latency-critical loops where cudaMalloc/cudaFree would
+ * synchronise the device.  It needs no context and allocates nothing: the
+ * ensemble (dev_loops, float32 [Nl][ppl][4]), the instances and the outputs
+ * are the caller's device buffers (layouts as wl_eval), and the scratch --
+ * instance constants and FP64 partial sums -- lives in one fixed 32 MiB
+ * device array inside the library, which every GPU that loads the library
+ * holds until the process exits.  Requests that need more scratch than that
+ * (about n_chunks * nF * 3 * ninst * 8 bytes, n_chunks = Nl / 8 for 32 or more
+ * instances, Nl otherwise) are rejected with WL_ERR_INVALID and a message on
+ * stderr; split them into smaller batches.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  Runs on `stream` (a cudaStream_t, NULL for
+ * the default stream) and returns when the outputs are written.  All calls
+ * share the one array, which keeps the last call's contents: calls that
+ * overlap on the GPU (other host threads, other streams) race. */
+int wl_eval_noalloc(const float *dev_loops, int Nl, int ppl, const wl_field *field,
+                    int ninst, const double *dev_cx, const double *dev_cy,
+                    const double *dev_T, int nF, const double *host_F, int group,
+                    double *dev_out_group, double *dev_out_mean, double *dev_out_sem,
+                    void *stream);
+
 /* the context's CUDA stream (a cudaStream_t), for timing and interop */
 int wl_ctx_stream(wl_ctx *ctx, void **stream);
 

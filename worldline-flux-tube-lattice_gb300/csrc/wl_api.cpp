@@ -858,3 +858,18 @@ double EV(double T, void *p, int *WLlist) {
 
 }  // extern "C"
 #pragma GCC visibility pop
+
+// Helpers shared with the allocation-free entry point (wl_noalloc.cu): the
+// same field validation, flux constants and loop partition as wl_eval_device.
+namespace wl {
+int shared_field_to_dev(const wl_field *f, int *kprofile, FieldDev *d) {
+  return field_to_dev(nullptr, f, kprofile, d);
+}
+void shared_fill_flux(SweepArgs &a, const wl_field *f, int nF, const double *F) {
+  fill_flux(a, f, nF, F);
+}
+void shared_fill_flux(LoopArgs &a, const wl_field *f, int nF, const double *F) {
+  fill_flux(a, f, nF, F);
+}
+int shared_plan_chunk(int group) { return plan_chunk(group); }
+}  // namespace wl

@@ -96,6 +96,8 @@ def lib():
                                      C.c_int, dp, C.c_int, vp, vp, vp]
         L.wl_ctx_stream.argtypes = [vp, C.POINTER(vp)]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
+        L.wl_eval_noalloc.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Field), C.c_int, vp, vp,
+                                      vp, C.c_int, dp, C.c_int, vp, vp, vp, vp]
         L.wl_loops.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_double,
                                C.c_double, C.c_double, fp, fp]
         L.wl_last_launches.argtypes = [vp, ip, C.POINTER(C.c_char_p)]
@@ -237,6 +239,23 @@ class Context:
 
     def synchronize(self):
         self._check(lib().wl_ctx_synchronize(self._h))
+
+
+def eval_noalloc(dev_loops: int, Nl: int, ppl: int, fld: Field, ninst: int, dev_cx: int,
+                 dev_cy: int, dev_T: int, F, group: int = 128, dev_out_group: int = 0,
+                 dev_out_mean: int = 0, dev_out_sem: int = 0, stream: int = 0):
+    """wl_eval_noalloc: the batched evaluation for callers that cannot let the
+    library allocate device memory (all buffers are the caller's device
+    pointers, given as integers; scratch is a fixed 32 MiB array in the
+    library).  Raises WlError on a non-zero status."""
+    F = _d(F)
+    st = lib().wl_eval_noalloc(C.c_void_p(dev_loops), Nl, ppl, C.byref(fld), ninst,
+                               C.c_void_p(dev_cx), C.c_void_p(dev_cy), C.c_void_p(dev_T), len(F),
+                               _p(F, C.c_double), group, C.c_void_p(dev_out_group or None),
+                               C.c_void_p(dev_out_mean or None), C.c_void_p(dev_out_sem or None),
+                               C.c_void_p(stream or None))
+    if st != 0:
+        raise WlError(st, "wl_eval_noalloc")
 
 
 def legacy_configure(profile="smooth", tubedist=1.0, lmin=None, nint=50,
