@@ -81,6 +81,14 @@ def dist_setup():
     return world, rank, local
 
 
+def shard(n, rank, world):
+    """Contiguous slice [lo, hi) of n independent units owned by `rank` (the
+    path needs no exchange between shards)."""
+    base, extra = divmod(n, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
 def max_over_ranks(x, world):
     if world == 1:
         return x

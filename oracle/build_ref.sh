@@ -7,7 +7,9 @@
 #   oracle/build_ref.sh [REFERENCE_DIR]      (default /root/reference)
 #
 # Outputs oracle/_ref/ref_driver_<profile> for the intEV.cu profiles and
-# oracle/_ref/ref_driver_ff for intEVff.cu (fixflux, spinor).  Exits 0 without
+# oracle/_ref/ref_driver_ff for intEVff.cu (fixflux, spinor), and the GPU
+# kernels oracle/_ref/ref_<case>.cubin (sm_103a device code of intEV.cu /
+# intEVff.cu with the reference's own -prec-div=false -prec-sqrt=false).  Exits 0 without
 # building when the reference tree is absent.
 set -euo pipefail
 REF=${1:-/root/reference}
@@ -37,7 +39,22 @@ build_one() {  # name, kernel source, profile, extra defines
     "$o.integrand.o" "$o.tint.o" -lm
 }
 
+# the reference kernel itself for the GPU (device code only, its own
+# fast-math flags): loaded at run time by oracle/ref_gpu.cu
+build_cubin() {  # name, kernel source, profile, lattice spacing, extra defines
+  local name=$1 src=$2 prof=$3 a=$4 extra=$5
+  "$NVCC" -cubin -O3 -arch sm_103a -prec-div=false -prec-sqrt=false -w -Dprofile=$prof \
+    -DWLREF_TUBEDIST=${a}f $extra $SHIM "$REF/$src" -o "$OUT/ref_$name.cubin"
+}
+
 pids=()
+for prof in step smooth quadratic gaussian; do
+  build_cubin "$prof" intEV.cu "$prof" 1.0 "" & pids+=($!)
+done
+build_cubin periodic_a1 intEV.cu periodic 1.0 "" & pids+=($!)
+build_cubin periodic_a2 intEV.cu periodic 2.0 "" & pids+=($!)
+build_cubin fixflux_a2 intEV.cu fixflux 2.0 "" & pids+=($!)
+build_cubin ff_a2 intEVff.cu fixflux 2.0 "-DWLREF_FF" & pids+=($!)
 for prof in step smooth quadratic gaussian periodic fixflux; do
   build_one "$prof" intEV.cu "$prof" "" & pids+=($!)
 done

@@ -57,6 +57,26 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+REF_DIR = os.path.join(HERE, "_ref")
+REF_GPU_LIB = os.path.join(HERE, "libref_gpu.so")
+
+
+def build_ref_gpu() -> str | None:
+    """Loader of the reference's own GPU kernel (needs nvcc); None without."""
+    import shutil
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = os.path.join(HERE, "ref_gpu.cu")
+    if not os.path.exists(nvcc):
+        return None
+    if os.path.exists(REF_GPU_LIB) and os.path.getmtime(REF_GPU_LIB) >= os.path.getmtime(src):
+        return REF_GPU_LIB
+    tmp = REF_GPU_LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call([nvcc, "-shared", "-Xcompiler", "-fPIC", "-O2", src, "-o", tmp])
+    os.replace(tmp, REF_GPU_LIB)
+    return REF_GPU_LIB
+
+
 _lib = None
 
 
