@@ -300,35 +300,36 @@ def main():
     except (OSError, KeyError, ValueError):
         pass
     # ---- end to end through the C ABI with host buffers --------------------
+    # the call a user makes for this workload: upload the ensemble, then
+    # wl_tint -- <W> on all (rho, T), FP64 proper-time integral with the
+    # counterterms, jackknife over 20 bins -> L_eff(rho, F) +- error on the host
     e2e = None
+    leff_summary = None
     if not args.no_e2e:
         host_loops = ctx.download(h)
-        groups = np.empty((ninst, len(FLUX), ng))
-        mean = np.empty((ninst, len(FLUX)))
-        sem = np.empty((ninst, len(FLUX)))
-        import ctypes as C
-
-        L = wltube.lib()
+        rho = np.unique(cx)
+        Tg = np.unique(T)
 
         def e2e_step():
             hh = ctx.upload(host_loops)
-            ctx._check(L.wl_eval(ctx.handle, hh, C.byref(fld), ninst,
-                                 wltube._p(cx, C.c_double), wltube._p(cy, C.c_double),
-                                 wltube._p(T, C.c_double), len(FLUX),
-                                 wltube._p(np.array(FLUX), C.c_double), GROUP,
-                                 wltube._p(groups, C.c_double), wltube._p(mean, C.c_double),
-                                 wltube._p(sem, C.c_double)))
+            out = ctx.tint(hh, fld, rho, Tg, FLUX, GROUP, nbins=20)
             ctx.release(hh)
+            return out
 
         e2e_step()
         barrier(world)
         s0 = time.perf_counter()
         for _ in range(args.steps):
-            e2e_step()
+            leff, lerr, _ = e2e_step()
         e2e_s = max_over_ranks(time.perf_counter() - s0, world)
         e2e = {"value": world * segs_step * args.steps / e2e_s, "unit": "segments/s",
-               "h2d_bytes_per_step": int(host_loops.nbytes + 3 * 8 * ninst),
-               "d2h_bytes_per_step": int(groups.nbytes + mean.nbytes + sem.nbytes)}
+               "api": "wl_ensemble_upload + wl_tint (L_eff with jackknife) + release",
+               "h2d_bytes_per_step": int(host_loops.nbytes + 8 * (len(rho) + len(Tg) + 3)),
+               "d2h_bytes_per_step": int(leff.nbytes + lerr.nbytes)}
+        leff_summary = {"rho": [float(rho[0]), float(rho[len(rho) // 8])],
+                        "F": FLUX[1],
+                        "L_eff": [float(leff[0, 1]), float(leff[len(rho) // 8, 1])],
+                        "jackknife_err": [float(lerr[0, 1]), float(lerr[len(rho) // 8, 1])]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, cores, sample = cpu_sample(seconds_target=args.cpu_seconds)
@@ -357,7 +358,8 @@ def main():
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
             "kernel_ms": per_launch_ms,
         },
-        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
+        "e2e": e2e, "L_eff_sample": leff_summary, "cpu_baseline": cpu,
+        "gpu_launches": launches, "clocks": clk,
     }
     print(json.dumps(line))
     ctx.release(h)

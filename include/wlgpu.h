@@ -108,6 +108,21 @@ int wl_eval(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
             int nF, const double *host_F, int group, double *out_group,
             double *out_mean, double *out_sem);
 
+/* Effective action density per centre of mass: for nrho radii rho[r] (centre
+ * of mass (rho, 0), as rhogrand sets it, EffAct.c:21-25) and a log-spaced
+ * proper-time grid T[0..nT-1] (ascending, nT >= 3), evaluates <W> on all
+ * nrho*nT instances, then in FP64 on the device: the integrand of Tfunc
+ * (Integrand.c:195-316; small-T series, constant-field and large-T forms,
+ * else e^{-m^2 T}/T^3 (<W> - 1 + (eTB)^2/6) scalar / (<W> - 1 - (eTB)^2/3)
+ * spinor with m^2 = 1, e = 0.30282212), Simpson over ln T on the grid, and
+ *   out_leff[r*nF + j] = <I>/(4 pi) (spinor) or <I>/(-2 pi) (scalar)
+ * (Tint.c:69-72), with out_err the jackknife error over nbins bins of the
+ * Nl/group loop groups (nbins must divide Nl/group).  out_igrand (may be
+ * NULL) receives the integrand [r][j][k][group]. */
+int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const double *host_rho,
+            int nT, const double *host_T, int nF, const double *host_F, int group, int nbins,
+            double *out_leff, double *out_err, double *out_igrand);
+
 /* Asynchronous variant on the context's stream for device-resident inputs and
  * outputs: dev_cx, dev_cy, dev_T [ninst] and the outputs are device pointers
  * (FP64, same layouts as wl_eval; outputs may be NULL), host_F stays a host

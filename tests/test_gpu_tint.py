@@ -1,0 +1,83 @@
+"""The FP64 proper-time integral (wl_tint) against the same integral built
+from the FP64 oracle: Tfunc's regimes and counterterms (Integrand.c:195-316),
+Simpson over ln T, Tintout's normalisation (Tint.c:69-72) and a jackknife
+over bins of loop groups."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def log_simpson_weights(T):
+    n = len(T)
+    du = np.log(T[1]) - np.log(T[0])
+    w = np.zeros(n)
+    m = n - 1
+    m13 = m if m % 2 == 0 else m - 3
+    for k in range(0, m13, 2):
+        w[k:k + 3] += np.array([1, 4, 1]) * du / 3
+    if m13 < m:
+        w[m13:m13 + 4] += np.array([3, 9, 9, 3]) * du / 8
+    return w * T
+
+
+def oracle_tint(loops, rho, T, F, fld, nbins):
+    cx = np.repeat(rho, len(T))
+    TT = np.tile(T, len(rho))
+    g = O.eval_groups(loops, cx, 0 * cx, TT, F, fld)          # [inst][F][ng]
+    ng = g.shape[2]
+    ig = np.zeros((len(rho), len(F), len(T), ng))
+    for r, x in enumerate(rho):
+        for j, f in enumerate(F):
+            for k, t in enumerate(T):
+                reg, an = O.tfunc_regime(t, x, 0.0, f, fld)
+                if reg == 3:
+                    ig[r, j, k] = [O.tfunc_mc(t, W, x, 0.0, f, fld) for W in g[r * len(T) + k, j]]
+                else:
+                    ig[r, j, k] = an
+    I = np.einsum("rjkg,k->rjg", ig, log_simpson_weights(T))
+    per = ng // nbins
+    mean = I.mean(axis=2)
+    binsum = I.reshape(len(rho), len(F), nbins, per).sum(axis=3)
+    loo = (I.sum(axis=2)[..., None] - binsum) / (ng - per)
+    jk = np.sqrt((nbins - 1) / nbins * ((loo - mean[..., None]) ** 2).sum(axis=2))
+    norm = 1 / (4 * np.pi) if fld.fermion else -1 / (2 * np.pi)
+    return mean * norm, jk * abs(norm), ig
+
+
+@pytest.mark.parametrize("fermion", [0, 1])
+def test_tint_matches_oracle_within_error_bars(fermion):
+    import wltube
+
+    loops = O.vloops(8, 512, 128)
+    rho = np.array([0.0, 0.5, 1.5], dtype=np.float32).astype(np.float64)
+    rt = np.sqrt(np.geomspace(1e-3, 1e2, 33)).astype(np.float32).astype(np.float64)
+    T = rt * rt
+    T = np.exp(np.linspace(np.log(T[0]), np.log(T[-1]), len(T)))  # exactly log-spaced
+    F = [0.5, 1.0]
+    with wltube.Context(0) as ctx:
+        h = ctx.upload(loops)
+        leff, err, ig = ctx.tint(h, wltube.field("smooth", fermion=fermion, nint=4), rho, T, F,
+                                 group=128, nbins=4, want_igrand=True)
+        ctx.release(h)
+    # the oracle at the instances the FP32 kernel represents exactly
+    rtf = np.sqrt(T).astype(np.float32).astype(np.float64)
+    ref_leff, ref_err, ref_ig = oracle_tint(loops, rho, rtf * rtf, F,
+                                            O.field("smooth", fermion=fermion, nint=4), 4)
+    assert np.all(np.isfinite(leff)) and np.all(err > 0)
+    # numerical difference far inside the Monte Carlo error bars
+    assert np.all(np.abs(leff - ref_leff) <= 0.05 * ref_err + 1e-12)
+    np.testing.assert_allclose(err, ref_err, rtol=0.05, atol=1e-12)
+
+
+def test_tint_rejects_non_log_grid():
+    import wltube
+
+    loops = O.vloops(8, 256, 16)
+    with wltube.Context(0) as ctx:
+        h = ctx.upload(loops)
+        with pytest.raises(wltube.WlError):
+            ctx.tint(h, wltube.field("smooth"), [0.0], [0.1, 0.2, 0.4, 0.5], [1.0], nbins=2)
+        ctx.release(h)

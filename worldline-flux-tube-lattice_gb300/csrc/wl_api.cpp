@@ -65,6 +65,7 @@ struct wl_ctx {
   DevBuf<double> out;       // group values, means, SEMs
   DevBuf<int> status;       // device status word
   DevBuf<int> list;         // EV() loop list
+  DevBuf<double> aux;       // proper-time integral inputs and outputs
   std::vector<float> h_inst;
   std::string err;
   int last_launches = 0;
@@ -340,6 +341,7 @@ int wl_ctx_destroy(wl_ctx *ctx) {
   ctx->out.release();
   ctx->status.release();
   ctx->list.release();
+  ctx->aux.release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return WL_OK;
@@ -655,6 +657,123 @@ int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s) {
   cudaEventDestroy(e1);
   *ops_per_s = (double)blocks * threads * iters * 8.0 / (best * 1e-3);
   return WL_OK;
+}
+
+// Quadrature weights in T for Simpson's rule on u = ln T (dT = T du):
+// composite 1/3 rule, with the 3/8 rule on the last three intervals when the
+// interval count is odd; the trapezoid rule for a single interval.
+static void log_simpson_weights(const double *T, int n, double du, double *w) {
+  for (int k = 0; k < n; ++k) w[k] = 0.0;
+  const int m = n - 1;
+  if (m == 1) {
+    w[0] = w[1] = 0.5 * du;
+  } else {
+    const int m13 = (m % 2 == 0) ? m : m - 3;
+    for (int k = 0; k < m13; k += 2) {
+      w[k] += du / 3.0;
+      w[k + 1] += 4.0 * du / 3.0;
+      w[k + 2] += du / 3.0;
+    }
+    if (m13 < m) {
+      const int k = m13;
+      w[k] += 3.0 * du / 8.0;
+      w[k + 1] += 9.0 * du / 8.0;
+      w[k + 2] += 9.0 * du / 8.0;
+      w[k + 3] += 3.0 * du / 8.0;
+    }
+  }
+  for (int k = 0; k < n; ++k) w[k] *= T[k];
+}
+
+int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const double *host_rho,
+            int nT, const double *host_T, int nF, const double *host_F, int group, int nbins,
+            double *out_leff, double *out_err, double *out_igrand) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (!host_rho || !host_T || !out_leff || !out_err)
+    return fail(ctx, WL_ERR_INVALID, "NULL rho, T or output array");
+  if (nrho < 1 || nT < 3) return fail(ctx, WL_ERR_INVALID, "need nrho >= 1 and nT >= 3");
+  const double du = log(host_T[1]) - log(host_T[0]);
+  for (int k = 0; k < nT; ++k) {
+    if (!(host_T[k] > 0.0) || !isfinite(host_T[k]))
+      return fail(ctx, WL_ERR_INVALID, "T[%d] must be positive and finite", k);
+    if (k > 0 && fabs((log(host_T[k]) - log(host_T[k - 1])) - du) > 1e-9 * fmax(1.0, fabs(du)))
+      return fail(ctx, WL_ERR_INVALID, "T must be log-spaced (ascending, uniform in ln T)");
+  }
+  if (!(du > 0.0)) return fail(ctx, WL_ERR_INVALID, "T must be ascending");
+  Ensemble e;
+  int kprof;
+  FieldDev fd;
+  int r = eval_prologue(ctx, handle, field, nrho * nT, nF, host_F, group, &e, &kprof, &fd);
+  if (r) return r;
+  const int ng = e.Nl / group;
+  if (nbins < 2 || ng % nbins)
+    return fail(ctx, WL_ERR_INVALID, "nbins = %d must be >= 2 and divide the %d groups", nbins, ng);
+  const int ninst = nrho * nT;
+  std::vector<double> cx((size_t)ninst), cy((size_t)ninst, 0.0), TT((size_t)ninst);
+  for (int i = 0; i < nrho; ++i)
+    for (int k = 0; k < nT; ++k) {
+      cx[(size_t)i * nT + k] = host_rho[i];
+      TT[(size_t)i * nT + k] = host_T[k];
+    }
+  if ((r = upload_instances(ctx, ninst, cx.data(), cy.data(), TT.data(), e.ppl))) return r;
+  WL_CHECK(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+  const size_t nout = (size_t)ninst * nF * (ng + 2);
+  if (ctx->out.reserve(nout) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu outputs", nout);
+  }
+  double *dg = ctx->out.p;
+  if ((r = run_eval(ctx, e, kprof, fd, field, ninst, nF, host_F, group, dg, nullptr, nullptr)))
+    return r;
+  // aux: rho | T | w | F | Ig | leff | err | igrand
+  const size_t n_ig = (size_t)nrho * nF * ng, n_le = (size_t)nrho * nF;
+  const size_t n_igr = out_igrand ? (size_t)nrho * nF * nT * ng : 0;
+  const size_t naux = (size_t)nrho + 2 * (size_t)nT + nF + n_ig + 2 * n_le + n_igr;
+  if (ctx->aux.reserve(naux) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate the proper-time buffers");
+  }
+  std::vector<double> h((size_t)nrho + 2 * (size_t)nT + nF);
+  memcpy(h.data(), host_rho, sizeof(double) * nrho);
+  memcpy(h.data() + nrho, host_T, sizeof(double) * nT);
+  log_simpson_weights(host_T, nT, du, h.data() + nrho + nT);
+  memcpy(h.data() + nrho + 2 * nT, host_F, sizeof(double) * nF);
+  WL_CHECK(ctx, cudaMemcpyAsync(ctx->aux.p, h.data(), sizeof(double) * h.size(),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  wl::TintArgs ta;
+  memset(&ta, 0, sizeof(ta));
+  double *d = ctx->aux.p;
+  ta.groups = dg;
+  ta.rho = d;
+  ta.T = d + nrho;
+  ta.w = d + nrho + nT;
+  ta.F = d + nrho + 2 * nT;
+  ta.Ig = d + nrho + 2 * nT + nF;
+  ta.leff = ta.Ig + n_ig;
+  ta.err = ta.leff + n_le;
+  ta.igrand = out_igrand ? ta.err + n_le : nullptr;
+  ta.nrho = nrho;
+  ta.nT = nT;
+  ta.nF = nF;
+  ta.ng = ng;
+  ta.nbins = nbins;
+  ta.profile = kprof;
+  ta.fermion = field->fermion != 0;
+  ta.l2 = field->lambda2;
+  ta.a = field->tubedist;
+  ta.lmin = field->lmin;
+  ta.m2 = 1.0;         // Integrand.c:12
+  ta.e = 0.30282212;   // Integrand.c:14
+  WL_CHECK(ctx, wl::launch_tint(ta, ctx->stream));
+  ctx->last_launches = 4;
+  WL_CHECK(ctx, cudaMemcpyAsync(out_leff, ta.leff, sizeof(double) * n_le, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  WL_CHECK(ctx, cudaMemcpyAsync(out_err, ta.err, sizeof(double) * n_le, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  if (out_igrand)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_igrand, ta.igrand, sizeof(double) * n_igr,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  return check_status(ctx);
 }
 
 int wl_ctx_stream(wl_ctx *ctx, void **stream) {

@@ -326,19 +326,21 @@ __device__ __forceinline__ df df_add(df x, df y) {
 }
 __device__ __forceinline__ df df_scale2(df x, float p2) { return {x.hi * p2, x.lo * p2}; }
 
-// cos(x.hi + x.lo): Cody-Waite reduction by 2 pi = C1 + C2 + C3 (Cody and
-// Waite, Software Manual for the Elementary Functions, 1980); C1 = 6.28125
-// has 8 significant bits, so k*C1 is exact for |k| < 2^16 and x.hi - k*C1 is
-// exact by Sterbenz's lemma; then cos(r + e) = cos r - e sin r.
-__device__ __forceinline__ float cos_df(df x) {
+// cos(x.hi + x.lo) - 1, accurate relative to the deviation itself (small
+// phases give W - 1 ~ 1e-9 that the proper-time integrand needs, Tint.c).
+// Cody-Waite reduction by 2 pi = C1 + C2 + C3 (Cody and Waite, Software
+// Manual for the Elementary Functions, 1980): C1 = 6.28125 has 8 significant
+// bits, so k*C1 is exact for |k| < 2^16 and x.hi - k*C1 is exact (Sterbenz);
+// then with s, c = sin, cos of r/2:  cos(r + e) - 1 = -2 s^2 - 2 s c e.
+__device__ __forceinline__ float cosm1_df(df x) {
   const float k = rintf(x.hi * 0.15915494f);
   const float t = fmaf(-k, 6.28125f, x.hi);
   const float u = fmaf(-k, 1.9353071693331003e-3f, x.lo);
   df r = two_sum(t, u);
   r.lo = fmaf(-k, 1.0253131677018246e-11f, r.lo);
   float sn, cs;
-  sincosf(r.hi, &sn, &cs);
-  return fmaf(-sn, r.lo, cs);
+  sincosf(0.5f * r.hi, &sn, &cs);
+  return -2.0f * sn * fmaf(cs, r.lo, sn);
 }
 
 // The reference's sentinel: C abs() of a double truncates to int
@@ -349,41 +351,52 @@ __device__ __forceinline__ bool sentinel600(float x) {
   return ax >= 601.0f && ax < 2147483648.0f;
 }
 
-// cosh(x.hi + x.lo) in FP64 range: below |x| = 80 from FP32 exp of the high
-// part, cosh(a + e) = cosh a + e sinh a; above, FP64 exp (FP32 overflows near
-// 89 while the reference's FP64 cosh is finite up to 710).
-__device__ __forceinline__ double cosh_df(df x) {
+// cosh(x.hi + x.lo) - 1 in FP64 range.  Below |x| = 80 from FP32:
+// cosh(a + e) - 1 = 2 sinh^2(a/2) + e sinh a, accurate for small a; above,
+// FP64 exp (FP32 overflows near 89 while the reference's FP64 cosh is finite
+// up to 710).
+__device__ __forceinline__ double coshm1_df(df x) {
   const float a = fabsf(x.hi), e = x.hi < 0.0f ? -x.lo : x.lo;
   if (a < 80.0f) {
-    const float ex = expf(a), iex = 1.0f / ex;
-    return (double)fmaf(0.5f * (ex - iex), e, 0.5f * (ex + iex));
+    const float sh = sinhf(0.5f * a);
+    const float ch = sqrtf(fmaf(sh, sh, 1.0f));
+    // sinh a = 2 sinh(a/2) cosh(a/2)
+    return (double)fmaf(2.0f * sh * ch, e, 2.0f * sh * sh);
   }
-  return 0.5 * exp((double)a + (double)e);
+  return 0.5 * exp((double)a + (double)e) - 1.0;
 }
 
 // Per-loop factors of EVMean (Integrand.c:352-390) from the sub-loop phases
-// p[k] and spin exponents q[k] (k: N/2, N/4b, N/4a):
+// p[k] and spin exponents q[k] (k: N/2, N/4b, N/4a), returned as deviations
+// d = w - 1 (the sums of deviations keep <W> - 1 accurate):
 //   w0 = W_N   = cos(p0/2 + (p1+p2)/4) [* cosh(same of q)]
 //   w1 = W_N/2 = cos(p0)                [* cosh(q0)]
 //   w2 = W_N/4 = cos((p1+p2)/2)         [* cosh(same of q)]
 // with the reference's 1e10 sentinel when a spin exponent truncates above 600.
 template <bool FERM>
-__device__ __forceinline__ void wfactors(const df p[3], const df q[3], double &w0, double &w1,
-                                         double &w2) {
+__device__ __forceinline__ void wfactors(const df p[3], const df q[3], double &d0, double &d1,
+                                         double &d2) {
   const df nb4 = df_add(p[1], p[2]);
-  w0 = (double)cos_df(df_add(df_scale2(p[0], 0.5f), df_scale2(nb4, 0.25f)));
-  w1 = (double)cos_df(p[0]);
-  w2 = (double)cos_df(df_scale2(nb4, 0.5f));
+  const float c0 = cosm1_df(df_add(df_scale2(p[0], 0.5f), df_scale2(nb4, 0.25f)));
+  const float c1 = cosm1_df(p[0]);
+  const float c2 = cosm1_df(df_scale2(nb4, 0.5f));
+  d0 = c0;
+  d1 = c1;
+  d2 = c2;
   if (FERM) {
     const df nb4f = df_add(q[1], q[2]);
     if (sentinel600(nb4f.hi) || sentinel600(q[0].hi)) {
-      w0 *= 1.0e10;
-      w1 *= 1.0e10;
-      w2 *= 1.0e10;
+      d0 = (1.0 + (double)c0) * 1.0e10 - 1.0;
+      d1 = (1.0 + (double)c1) * 1.0e10 - 1.0;
+      d2 = (1.0 + (double)c2) * 1.0e10 - 1.0;
     } else {
-      w0 *= cosh_df(df_add(df_scale2(q[0], 0.5f), df_scale2(nb4f, 0.25f)));
-      w1 *= cosh_df(q[0]);
-      w2 *= cosh_df(df_scale2(nb4f, 0.5f));
+      // cos * cosh - 1 = (cos - 1) cosh + (cosh - 1)
+      const double h0 = coshm1_df(df_add(df_scale2(q[0], 0.5f), df_scale2(nb4f, 0.25f)));
+      const double h1 = coshm1_df(q[0]);
+      const double h2 = coshm1_df(df_scale2(nb4f, 0.5f));
+      d0 = (double)c0 * (1.0 + h0) + h0;
+      d1 = (double)c1 * (1.0 + h1) + h1;
+      d2 = (double)c2 * (1.0 + h2) + h2;
     }
   }
 }
@@ -393,8 +406,8 @@ __device__ __forceinline__ void wfactors(const df p[3], const df q[3], double &w
 // (without h/3 and the f' scale).  Per flux value j, cph_j = F_j h/3 and
 // csp_j = F_j h/3 fp_scale are double-float constants and tq = 4T/N is the
 // instance's, so the phase is F G h/3 and the spin exponent 2 F T sum/(N/2)
-// (N/2 loop) or 2 F T sum/(N/4) (N/4 loops).  add(j, w0, w1, w2) receives the
-// W factors (accumulated in FP64 by the caller).
+// (N/2 loop) or 2 F T sum/(N/4) (N/4 loops).  add(j, d0, d1, d2) receives the
+// W factors minus one (accumulated in FP64 by the caller).
 template <bool FERM, class Add>
 __device__ __forceinline__ void loop_epilogue(const df G[3], const df H[3], const float *cph_hi,
                                               const float *cph_lo, const float *csp_hi,

@@ -89,6 +89,22 @@ cudaError_t launch_instance_setup(const double *cx, const double *cy, const doub
 cudaError_t launch_peak_probe(int kind, int blocks, int threads, int iters, float *sink,
                               cudaStream_t s);
 
+// FP64 proper-time integral + jackknife (wl_tint.cu)
+struct TintArgs {
+  const double *groups;  // [nrho * nT][nF][ng]   instance i = r * nT + k
+  const double *rho;     // [nrho] centre of mass x (y = 0, as rhogrand, EffAct.c:23-25)
+  const double *T;       // [nT]
+  const double *w;       // [nT] quadrature weights in T (dT, Simpson on ln T)
+  const double *F;       // [nF]
+  int nrho, nT, nF, ng, nbins;
+  int profile, fermion;
+  double l2, a, lmin, m2, e;
+  double *igrand;  // optional [nrho][nF][nT][ng]
+  double *Ig;      // [nrho][nF][ng]
+  double *leff, *err;  // [nrho][nF]
+};
+cudaError_t launch_tint(const TintArgs &a, cudaStream_t s);
+
 // seeded unit loops
 cudaError_t launch_vloops(uint64_t seed, int first, int Nl, int ppl, float4 *out,
                           cudaStream_t s);

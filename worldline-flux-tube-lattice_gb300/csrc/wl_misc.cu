@@ -45,7 +45,8 @@ cudaError_t launch_loopwarp(int profile, bool fermion, int nint, const LoopArgs 
 // in chunk order (the result of an instance does not depend on how many
 // other instances share the launch), the Richardson combination
 // 8/3 W_N - 2 W_N/2 + 1/3 W_N/4 (Integrand.c:400), then mean and standard
-// error over the groups.
+// error over the groups.  The partial sums hold W - 1 per loop; the weights
+// sum to one, so <W> = 1 + the same combination of the deviations.
 __global__ void group_reduce_kernel(const double *__restrict__ partial, int n_chunks,
                                     int cpg, int lpg, int ninst, int nF,
                                     double *__restrict__ out_group,
@@ -64,7 +65,7 @@ __global__ void group_reduce_kernel(const double *__restrict__ partial, int n_ch
       s1 += partial[base + ninst];
       s2 += partial[base + 2 * (size_t)ninst];
     }
-    return 8.0 / 3.0 * (s0 * inv) - 2.0 * (s1 * inv) + 1.0 / 3.0 * (s2 * inv);
+    return 1.0 + (8.0 / 3.0 * (s0 * inv) - 2.0 * (s1 * inv) + 1.0 / 3.0 * (s2 * inv));
   };
   double mean = 0.0;
   for (int g = 0; g < ng; ++g) {
@@ -92,7 +93,8 @@ cudaError_t launch_group_reduce(const double *partial, int n_chunks, int cpg, in
   return cudaGetLastError();
 }
 
-// EV(): mean of the per-loop factors over an index list, fixed-order tree.
+// EV(): mean of the per-loop factors (stored as W - 1) over an index list,
+// fixed-order tree.
 constexpr int kListThreads = 128;
 __global__ void __launch_bounds__(kListThreads)
     list_mean_kernel(const double *__restrict__ w, const int *__restrict__ list, int n,
@@ -116,8 +118,8 @@ __global__ void __launch_bounds__(kListThreads)
   }
   if (threadIdx.x == 0) {
     const double inv = 1.0 / (double)n;
-    out[0] = 8.0 / 3.0 * (red[0][0] * inv) - 2.0 * (red[1][0] * inv) +
-             1.0 / 3.0 * (red[2][0] * inv);
+    out[0] = 1.0 + (8.0 / 3.0 * (red[0][0] * inv) - 2.0 * (red[1][0] * inv) +
+                    1.0 / 3.0 * (red[2][0] * inv));
   }
 }
 

@@ -95,6 +95,8 @@ def lib():
         L.wl_eval_device.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, vp, vp, vp,
                                      C.c_int, dp, C.c_int, vp, vp, vp]
         L.wl_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+        L.wl_tint.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, C.c_int, dp, C.c_int, dp,
+                              C.c_int, C.c_int, dp, dp, dp]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
         L.wl_eval_noalloc.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Field), C.c_int, vp, vp,
                                       vp, C.c_int, dp, C.c_int, vp, vp, vp, vp]
@@ -209,6 +211,23 @@ class Context:
             C.c_void_p(dev_T), len(F), _p(F, C.c_double), group,
             C.c_void_p(dev_out_group or None), C.c_void_p(dev_out_mean or None),
             C.c_void_p(dev_out_sem or None)))
+
+    def tint(self, handle: int, fld: Field, rho, T, F, group: int = 128, nbins: int = 20,
+             want_igrand: bool = False):
+        """Effective action density per radius (wl_tint): L_eff[nrho][nF], its
+        jackknife error, and optionally the integrand [nrho][nF][nT][ng]."""
+        rho, T, F = _d(rho), _d(T), _d(F)
+        Nl = C.c_int()
+        self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), None))
+        ng = Nl.value // group
+        leff = np.empty((len(rho), len(F)))
+        err = np.empty((len(rho), len(F)))
+        ig = np.empty((len(rho), len(F), len(T), ng)) if want_igrand else None
+        self._check(lib().wl_tint(self._h, handle, C.byref(fld), len(rho), _p(rho, C.c_double),
+                                  len(T), _p(T, C.c_double), len(F), _p(F, C.c_double), group,
+                                  nbins, _p(leff, C.c_double), _p(err, C.c_double),
+                                  _p(ig, C.c_double) if want_igrand else None))
+        return leff, err, ig
 
     def peak_probe(self, kind: int) -> float:
         """Lane operations per second of the FP32 FMA (0) or MUFU rcp (1) pipe."""
