@@ -178,6 +178,53 @@ int wl_loops(wl_ctx *ctx, int handle, const wl_field *field, double cx, double c
  * which sweep kernel ("instance-parallel" or "loop-parallel"). */
 int wl_last_launches(wl_ctx *ctx, int *launches, const char **sweep_kind);
 
+/* ---- uneven batches in one persistent launch ---------------------------- */
+/* One evaluation job of a batch: instances of one ensemble and field. */
+typedef struct {
+  int handle;            /* ensemble                                         */
+  wl_field field;        /* step, smooth, quadratic or gaussian profile      */
+  int ninst;             /* instances (host arrays of ninst doubles)         */
+  const double *cx, *cy, *T;
+  int nF;                /* flux values (<= 4)                               */
+  double F[4];
+  int group;             /* loops per group (divides the ensemble's Nl)      */
+  double *out_group;     /* host outputs as wl_eval (any may be NULL)        */
+  double *out_mean, *out_sem;
+} wl_job;
+
+#define WL_BATCH_GRAPH 1 /* capture the device work as a CUDA graph and launch it */
+
+/* Evaluate njobs jobs of uneven size in one persistent launch: every CTA takes
+ * (job, instance tile, loop chunk) tiles from a device queue ordered by
+ * decreasing cost; a job's results are identical to those it gets alone in a
+ * batch (the tile shape depends only on the job and the tuned parameters).
+ * The loops per tile come from the context's tuned points-per-tile target
+ * (wl_batch_autotune; default 16384), the persistent grid from its tuned CTAs
+ * per SM (default: the occupancy limit). */
+int wl_batch_eval(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags);
+
+/* Autotuner: times the batch for every candidate (points per tile in
+ * {4096, 8192, 16384, 32768, 65536} x persistent CTAs per SM in
+ * {occupancy - 1, occupancy}) and keeps the fastest in the context.  The
+ * chosen values are returned (pointers may be NULL). */
+int wl_batch_autotune(wl_ctx *ctx, int njobs, const wl_job *jobs, int *points_per_tile,
+                      int *ctas_per_sm);
+
+/* Statistics of the last wl_batch_eval: device time (ms, CUDA events around
+ * the persistent kernel and the reduction), tiles, persistent CTAs, points per
+ * tile. */
+int wl_batch_stats(wl_ctx *ctx, double *device_ms, int *ntiles, int *grid,
+                   int *points_per_tile);
+
+/* The plain per-instance kernel, the baseline of the batched path: one
+ * launch per instance with one thread per loop walking its points from
+ * global memory (the reference kernel's structure, intEV.cu:573-582), same
+ * arithmetic and outputs as wl_eval.  *device_ms receives the summed time. */
+int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
+                  const double *host_cx, const double *host_cy, const double *host_T,
+                  int nF, const double *host_F, int group, double *out_group,
+                  double *out_mean, double *out_sem, double *device_ms);
+
 /* ---- legacy EV() configuration ----------------------------------------- */
 /* The reference selects the profile at compile time (intT.h "profile"); the
  * library's EV() uses the profile, lattice spacing, Simpson intervals and

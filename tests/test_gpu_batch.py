@@ -1,0 +1,80 @@
+"""The persistent multi-job batch (wl_batch_eval), its CUDA-graph launch, the
+autotuner and the plain per-instance baseline kernel, against single-job
+evaluations and the FP64 oracle."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+W_TOL, W_FLOOR = 1e-5, 1e-2
+
+
+def werr(w, ref, scale=1.0):
+    return np.max(np.abs(w - ref) / np.maximum(np.abs(ref), W_FLOOR * scale))
+
+
+def f32_exact(cx, cy, T):
+    rt = np.sqrt(np.asarray(T, np.float64)).astype(np.float32).astype(np.float64)
+    return (np.asarray(cx, np.float32).astype(np.float64),
+            np.asarray(cy, np.float32).astype(np.float64), rt * rt)
+
+
+@pytest.fixture(scope="module")
+def setup():
+    import wltube
+
+    ctx = wltube.Context(0)
+    rng = np.random.default_rng(4)
+    ens = {(ppl, Nl): ctx.generate(4, Nl, ppl) for ppl, Nl in [(64, 256), (128, 256), (256, 512)]}
+    specs = [("smooth", 1, 4, 1.0, (64, 256), 200, [0.5, 1.0]),
+             ("gaussian", 1, 4, 0.5, (128, 256), 37, [2.0]),
+             ("smooth", 0, 8, 2.0, (256, 512), 140, [0.1, 0.3, 1.0]),
+             ("step", 0, 4, 3.0, (64, 256), 9, [1.0]),
+             ("quadratic", 1, 4, 1.5, (128, 256), 300, [0.7])]
+    jobs = []
+    for prof, fe, nint, l2, key, n, F in specs:
+        cx, cy, T = f32_exact(rng.uniform(0, 2.5, n), rng.uniform(-0.2, 0.2, n),
+                              np.exp(rng.uniform(np.log(0.02), np.log(3.0), n)))
+        jobs.append({"handle": ens[key], "field": wltube.field(prof, fermion=fe, nint=nint,
+                                                               lambda2=l2),
+                     "cx": cx, "cy": cy, "T": T, "F": F, "group": 128, "key": key,
+                     "ofield": O.field(prof, fermion=fe, nint=nint, lambda2=l2)})
+    yield ctx, jobs, ens
+    ctx.close()
+
+
+def test_batch_matches_oracle_and_single_jobs(setup):
+    ctx, jobs, ens = setup
+    outs = ctx.batch_eval(jobs, graph=True)
+    st = ctx.batch_stats()
+    assert st["tiles"] > 0 and st["grid"] > 0 and ctx.last_launches()[1] == "persistent-batch"
+    for j, (g, m, s) in zip(jobs, outs):
+        loops = ctx.download(j["handle"])
+        ref, S = O.eval_groups(loops, j["cx"], j["cy"], j["T"], j["F"], j["ofield"],
+                               return_scale=True)
+        assert werr(g, ref, S) < W_TOL
+        g1, _, _ = ctx.eval(j["handle"], j["field"], j["cx"], j["cy"], j["T"], j["F"])
+        assert werr(g, g1) < W_TOL
+
+
+def test_batch_results_do_not_depend_on_the_mix(setup):
+    ctx, jobs, _ = setup
+    mixed = ctx.batch_eval(jobs, graph=False)
+    for k in (0, 3):
+        alone = ctx.batch_eval([jobs[k]], graph=True)[0]
+        for a, b in zip(alone, mixed[k]):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_autotune_and_plain_baseline(setup):
+    ctx, jobs, _ = setup
+    pts, ctas = ctx.batch_autotune(jobs)
+    assert pts in (4096, 8192, 16384, 32768, 65536) and ctas >= 1
+    outs = ctx.batch_eval(jobs)
+    j = jobs[0]
+    g, m, s, ms = ctx.eval_plain(j["handle"], j["field"], j["cx"][:20], j["cy"][:20], j["T"][:20],
+                                 j["F"])
+    assert ms > 0 and ctx.last_launches() == (21, "plain-per-instance")
+    assert werr(g, outs[0][0][:20]) < W_TOL

@@ -26,7 +26,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 SOURCES = ["wl_sweep_smooth.cu", "wl_sweep_simple.cu", "wl_sweep_periodic.cu",
            "wl_sweep_fixflux.cu", "wl_misc.cu", "wl_api.cpp", "wl_noalloc.cu",
-           "wl_tint.cu"]
+           "wl_tint.cu", "wl_batch.cu"]
 
 
 def nvcc() -> str:

@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -66,6 +67,15 @@ struct wl_ctx {
   DevBuf<int> status;       // device status word
   DevBuf<int> list;         // EV() loop list
   DevBuf<double> aux;       // proper-time integral inputs and outputs
+  // batches: instances, partial sums, outputs, descriptors (jobs, tiles,
+  // reduce jobs, queue counter)
+  DevBuf<float> b_inst;
+  DevBuf<double> b_part, b_out;
+  DevBuf<unsigned char> b_meta;
+  int tune_points = 16384;  // points per tile target (autotuned)
+  int tune_ctas = 0;        // persistent CTAs per SM, 0 = occupancy limit
+  double last_batch_ms = 0.0;
+  int last_batch_tiles = 0, last_batch_grid = 0;
   std::vector<float> h_inst;
   std::string err;
   int last_launches = 0;
@@ -279,6 +289,242 @@ LegacyState &legacy() {
 }
 }  // namespace
 
+
+// ============================================================== batches ==
+extern "C" {
+static int eval_prologue(wl_ctx *ctx, int handle, const wl_field *field, int ninst, int nF,
+                         const double *host_F, int group, Ensemble *e, int *kprof,
+                         FieldDev *fd);
+}
+
+namespace {
+
+// loops per tile of a job: the largest divisor of its group size not above
+// points_per_tile / ppl (at least 1)
+int batch_loops_per_tile(int points_per_tile, int ppl, int group) {
+  int want = points_per_tile / ppl;
+  if (want < 1) want = 1;
+  int lc = want < group ? want : group;
+  while (group % lc) --lc;
+  return lc;
+}
+
+struct BatchPlan {
+  std::vector<wl::SweepArgs> jobs;
+  std::vector<wl::BatchTile> tiles;
+  std::vector<wl::ReduceJob> rjobs;
+  std::vector<float> inst;
+  size_t part_total = 0, out_total = 0;
+  int flat_total = 0;
+};
+
+int batch_plan(wl_ctx *ctx, int njobs, const wl_job *jobs, int points, BatchPlan *P) {
+  size_t inst_total = 0;
+  std::vector<size_t> inst_off(njobs), part_off(njobs), out_off(njobs);
+  std::vector<int> lcs(njobs), kprofs(njobs);
+  std::vector<FieldDev> fds(njobs);
+  for (int i = 0; i < njobs; ++i) {
+    const wl_job &J = jobs[i];
+    Ensemble e;
+    int r = eval_prologue(ctx, J.handle, &J.field, J.ninst, J.nF, J.F, J.group, &e, &kprofs[i],
+                          &fds[i]);
+    if (r) return fail(ctx, r, "job %d: %s", i, ctx->err.c_str());
+    if (!J.cx || !J.cy || !J.T) return fail(ctx, WL_ERR_INVALID, "job %d: NULL instance arrays", i);
+    if (!wl::batch_supports(kprofs[i], J.field.nint))
+      return fail(ctx, WL_ERR_INVALID, "job %d: profile %d is not supported in batches", i,
+                  J.field.profile);
+    lcs[i] = batch_loops_per_tile(points, e.ppl, J.group);
+    inst_off[i] = inst_total;
+    inst_total += (size_t)wl::kInstArrays * J.ninst;
+    part_off[i] = P->part_total;
+    P->part_total += (size_t)(e.Nl / lcs[i]) * J.nF * 3 * J.ninst;
+    out_off[i] = P->out_total;
+    P->out_total += (size_t)J.ninst * J.nF * (e.Nl / J.group + 2);
+  }
+  P->inst.resize(inst_total);
+  P->jobs.resize(njobs);
+  P->rjobs.resize(njobs);
+  P->tiles.clear();
+  for (int i = 0; i < njobs; ++i) {
+    const wl_job &J = jobs[i];
+    Ensemble e;
+    lookup(ctx, J.handle, &e);
+    for (int k = 0; k < J.ninst; ++k)
+      if (!isfinite(J.cx[k]) || !isfinite(J.cy[k]) || !(J.T[k] > 0.0) || !isfinite(J.T[k]))
+        return fail(ctx, WL_ERR_INVALID, "job %d instance %d: need finite centre and T > 0", i, k);
+    float *h = P->inst.data() + inst_off[i];
+    const int n = J.ninst;
+    for (int k = 0; k < n; ++k) {
+      const float rtT = (float)sqrt(J.T[k]);
+      const double tq = 4.0 * ((double)rtT * (double)rtT) / (double)e.ppl;
+      h[k] = (float)J.cx[k];
+      h[n + k] = (float)J.cy[k];
+      h[2 * n + k] = rtT;
+      h[3 * n + k] = (float)tq;
+      h[4 * n + k] = (float)(tq - (double)(float)tq);
+    }
+    wl::SweepArgs &a = P->jobs[i];
+    memset(&a, 0, sizeof(a));
+    a.loops = e.dev;
+    a.Nl = e.Nl;
+    a.ppl = e.ppl;
+    a.ninst = n;
+    // device pointers are patched in after the buffers are sized (offsets now)
+    a.cx = (const float *)(uintptr_t)(inst_off[i]);
+    a.nF = J.nF;
+    fill_flux(a, &J.field, J.nF, J.F);
+    a.field = fds[i];
+    a.chunk_loops = lcs[i];
+    a.n_chunks = e.Nl / lcs[i];
+    a.partial = (double *)(uintptr_t)(part_off[i]);
+    a.wait_tries = 1u << 22;
+    a.kprof = kprofs[i];
+    a.fermion = J.field.fermion != 0;
+    a.nint = J.field.nint;
+    wl::ReduceJob &rj = P->rjobs[i];
+    rj.n_chunks = a.n_chunks;
+    rj.cpg = J.group / lcs[i];
+    rj.lpg = J.group;
+    rj.ninst = n;
+    rj.nF = J.nF;
+    rj.first = P->flat_total;
+    rj.out_group = (double *)(uintptr_t)(out_off[i]);
+    P->flat_total += n * J.nF;
+    const int tiles_x = (n + wl::kSweepThreads - 1) / wl::kSweepThreads;
+    const int cost = lcs[i] * e.ppl;
+    for (int c = 0; c < a.n_chunks; ++c)
+      for (int t = 0; t < tiles_x; ++t) P->tiles.push_back({i, t, c, cost});
+  }
+  // longest tiles first: the queue then drains evenly (LPT order); ties keep
+  // job order
+  std::stable_sort(P->tiles.begin(), P->tiles.end(),
+                   [](const wl::BatchTile &x, const wl::BatchTile &y) { return x.cost > y.cost; });
+  return WL_OK;
+}
+
+int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points, int ctas,
+              bool copy_out) {
+  BatchPlan P;
+  int r = batch_plan(ctx, njobs, jobs, points, &P);
+  if (r) return r;
+  if (P.tiles.empty()) return fail(ctx, WL_ERR_INVALID, "empty batch");
+  const size_t jobs_bytes = sizeof(wl::SweepArgs) * njobs;
+  const size_t tiles_bytes = sizeof(wl::BatchTile) * P.tiles.size();
+  const size_t rj_bytes = sizeof(wl::ReduceJob) * njobs;
+  const size_t off_tiles = (jobs_bytes + 255) & ~(size_t)255;
+  const size_t off_rj = (off_tiles + tiles_bytes + 255) & ~(size_t)255;
+  const size_t off_cnt = (off_rj + rj_bytes + 255) & ~(size_t)255;
+  const size_t meta_bytes = off_cnt + 256;
+  if (ctx->b_inst.reserve(P.inst.size()) != cudaSuccess ||
+      ctx->b_part.reserve(P.part_total) != cudaSuccess ||
+      ctx->b_out.reserve(P.out_total) != cudaSuccess ||
+      ctx->b_meta.reserve(meta_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate the batch buffers");
+  }
+  // patch offsets into device pointers
+  for (int i = 0; i < njobs; ++i) {
+    wl::SweepArgs &a = P.jobs[i];
+    const size_t io = (size_t)(uintptr_t)a.cx;
+    const int n = a.ninst;
+    a.cx = ctx->b_inst.p + io;
+    a.cy = a.cx + n;
+    a.rtT = a.cx + 2 * n;
+    a.tqh = a.cx + 3 * n;
+    a.tql = a.cx + 4 * n;
+    a.partial = ctx->b_part.p + (size_t)(uintptr_t)a.partial;
+    a.status = ctx->status.p;
+    wl::ReduceJob &rj = P.rjobs[i];
+    rj.partial = a.partial;
+    const int ng = a.Nl / rj.lpg;
+    rj.out_group = ctx->b_out.p + (size_t)(uintptr_t)rj.out_group;
+    rj.out_mean = rj.out_group + (size_t)n * rj.nF * ng;
+    rj.out_sem = rj.out_mean + (size_t)n * rj.nF;
+  }
+  unsigned char *meta = ctx->b_meta.p;
+  WL_CHECK(ctx, cudaMemcpyAsync(ctx->b_inst.p, P.inst.data(), sizeof(float) * P.inst.size(),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  WL_CHECK(ctx, cudaMemcpyAsync(meta, P.jobs.data(), jobs_bytes, cudaMemcpyHostToDevice, ctx->stream));
+  WL_CHECK(ctx, cudaMemcpyAsync(meta + off_tiles, P.tiles.data(), tiles_bytes,
+                                cudaMemcpyHostToDevice, ctx->stream));
+  WL_CHECK(ctx, cudaMemcpyAsync(meta + off_rj, P.rjobs.data(), rj_bytes, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  WL_CHECK(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));  // host vectors are released on return
+
+  wl::BatchArgs B;
+  B.jobs = (const wl::SweepArgs *)meta;
+  B.tiles = (const wl::BatchTile *)(meta + off_tiles);
+  B.ntiles = (int)P.tiles.size();
+  B.counter = (int *)(meta + off_cnt);
+  const int occ = wl::batch_max_ctas_per_sm();
+  const int per_sm = ctas > 0 && ctas <= occ ? ctas : occ;
+  int grid = per_sm * ctx->num_sms;
+  if (grid > B.ntiles) grid = B.ntiles;
+  const wl::ReduceJob *rjd = (const wl::ReduceJob *)(meta + off_rj);
+
+  cudaEvent_t e0, e1;
+  WL_CHECK(ctx, cudaEventCreate(&e0));
+  WL_CHECK(ctx, cudaEventCreate(&e1));
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(B.counter, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = wl::launch_batch(B, grid, ctx->stream);
+    if (e == cudaSuccess) e = wl::launch_batch_reduce(rjd, njobs, P.flat_total, ctx->stream);
+    return e;
+  };
+  cudaError_t ce = cudaEventRecord(e0, ctx->stream);
+  if (ce == cudaSuccess) {
+    if (flags & WL_BATCH_GRAPH) {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      ce = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+      if (ce == cudaSuccess) {
+        cudaError_t ce2 = enqueue();
+        ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (ce2 != cudaSuccess) ce = ce2;
+      }
+      if (ce == cudaSuccess) ce = cudaGraphInstantiate(&ge, g, 0);
+      if (ce == cudaSuccess) ce = cudaGraphLaunch(ge, ctx->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+      if (ge) cudaGraphExecDestroy(ge);
+      if (g) cudaGraphDestroy(g);
+    } else {
+      ce = enqueue();
+    }
+  }
+  if (ce == cudaSuccess) ce = cudaEventRecord(e1, ctx->stream);
+  if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  if (ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "batch launch");
+  ctx->last_batch_ms = ms;
+  ctx->last_batch_tiles = B.ntiles;
+  ctx->last_batch_grid = grid;
+  ctx->last_launches = 2;
+  ctx->last_kind = "persistent-batch";
+  if ((r = check_status(ctx))) return r;
+  if (!copy_out) return WL_OK;
+  std::vector<double> host(P.out_total);
+  WL_CHECK(ctx, cudaMemcpyAsync(host.data(), ctx->b_out.p, sizeof(double) * P.out_total,
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < njobs; ++i) {
+    const wl_job &J = jobs[i];
+    const wl::ReduceJob &rj = P.rjobs[i];
+    const int ng = P.jobs[i].Nl / J.group;
+    const size_t o = (size_t)(rj.out_group - ctx->b_out.p);
+    const size_t ngrp = (size_t)J.ninst * J.nF * ng, nm = (size_t)J.ninst * J.nF;
+    if (J.out_group) memcpy(J.out_group, host.data() + o, sizeof(double) * ngrp);
+    if (J.out_mean) memcpy(J.out_mean, host.data() + o + ngrp, sizeof(double) * nm);
+    if (J.out_sem) memcpy(J.out_sem, host.data() + o + ngrp + nm, sizeof(double) * nm);
+  }
+  return WL_OK;
+}
+
+}  // namespace
+
 // ================================================================ C ABI ==
 // Only the C entry points are exported (the build hides everything else).
 #pragma GCC visibility push(default)
@@ -342,6 +588,10 @@ int wl_ctx_destroy(wl_ctx *ctx) {
   ctx->status.release();
   ctx->list.release();
   ctx->aux.release();
+  ctx->b_inst.release();
+  ctx->b_part.release();
+  ctx->b_out.release();
+  ctx->b_meta.release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return WL_OK;
@@ -772,6 +1022,118 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
                                 ctx->stream));
   if (out_igrand)
     WL_CHECK(ctx, cudaMemcpyAsync(out_igrand, ta.igrand, sizeof(double) * n_igr,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  return check_status(ctx);
+}
+
+int wl_batch_eval(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (njobs < 1 || !jobs) return fail(ctx, WL_ERR_INVALID, "need njobs >= 1 jobs");
+  int r = set_device(ctx);
+  if (r) return r;
+  return batch_run(ctx, njobs, jobs, flags, ctx->tune_points, ctx->tune_ctas, true);
+}
+
+int wl_batch_autotune(wl_ctx *ctx, int njobs, const wl_job *jobs, int *points_per_tile,
+                      int *ctas_per_sm) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (njobs < 1 || !jobs) return fail(ctx, WL_ERR_INVALID, "need njobs >= 1 jobs");
+  int r = set_device(ctx);
+  if (r) return r;
+  const int occ = wl::batch_max_ctas_per_sm();
+  const int pts[5] = {4096, 8192, 16384, 32768, 65536};
+  double best = 1e300;
+  int bp = ctx->tune_points, bc = ctx->tune_ctas;
+  for (int c = (occ > 1 ? occ - 1 : 1); c <= occ; ++c)
+    for (int i = 0; i < 5; ++i) {
+      // one untimed pass, then the timed one
+      if ((r = batch_run(ctx, njobs, jobs, 0, pts[i], c, false))) return r;
+      if ((r = batch_run(ctx, njobs, jobs, 0, pts[i], c, false))) return r;
+      if (ctx->last_batch_ms < best) {
+        best = ctx->last_batch_ms;
+        bp = pts[i];
+        bc = c;
+      }
+    }
+  ctx->tune_points = bp;
+  ctx->tune_ctas = bc;
+  if (points_per_tile) *points_per_tile = bp;
+  if (ctas_per_sm) *ctas_per_sm = bc;
+  return WL_OK;
+}
+
+int wl_batch_stats(wl_ctx *ctx, double *device_ms, int *ntiles, int *grid, int *points_per_tile) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (device_ms) *device_ms = ctx->last_batch_ms;
+  if (ntiles) *ntiles = ctx->last_batch_tiles;
+  if (grid) *grid = ctx->last_batch_grid;
+  if (points_per_tile) *points_per_tile = ctx->tune_points;
+  return WL_OK;
+}
+
+int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst, const double *host_cx,
+                  const double *host_cy, const double *host_T, int nF, const double *host_F,
+                  int group, double *out_group, double *out_mean, double *out_sem,
+                  double *device_ms) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (!host_cx || !host_cy || !host_T) return fail(ctx, WL_ERR_INVALID, "NULL instance arrays");
+  Ensemble e;
+  int kprof;
+  FieldDev fd;
+  int r = eval_prologue(ctx, handle, field, ninst, nF, host_F, group, &e, &kprof, &fd);
+  if (r) return r;
+  if (!wl::batch_supports(kprof, field->nint))
+    return fail(ctx, WL_ERR_INVALID, "the plain kernel covers the step, smooth, quadratic and "
+                                     "gaussian profiles");
+  if ((r = upload_instances(ctx, ninst, host_cx, host_cy, host_T, e.ppl))) return r;
+  const int ng = e.Nl / group;
+  const size_t npart = (size_t)e.Nl * nF * 3 * ninst;
+  if (ctx->partial.reserve(npart) != cudaSuccess ||
+      ctx->out.reserve((size_t)ninst * nF * (ng + 2)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, WL_ERR_NOMEM, "cannot allocate the plain-kernel buffers");
+  }
+  wl::LoopArgs a;
+  memset(&a, 0, sizeof(a));
+  a.loops = e.dev;
+  a.Nl = e.Nl;
+  a.ppl = e.ppl;
+  a.ninst = ninst;
+  a.cx = ctx->inst.p;
+  a.cy = a.cx + ninst;
+  a.rtT = a.cx + 2 * ninst;
+  a.tqh = a.cx + 3 * ninst;
+  a.tql = a.cx + 4 * ninst;
+  a.nF = nF;
+  fill_flux(a, field, nF, host_F);
+  a.field = fd;
+  a.partial = ctx->partial.p;
+  cudaEvent_t e0, e1;
+  WL_CHECK(ctx, cudaEventCreate(&e0));
+  WL_CHECK(ctx, cudaEventCreate(&e1));
+  WL_CHECK(ctx, cudaEventRecord(e0, ctx->stream));
+  for (int i = 0; i < ninst; ++i)
+    WL_CHECK(ctx, wl::launch_plain(kprof, field->fermion != 0, field->nint, a, i, ctx->stream));
+  WL_CHECK(ctx, cudaEventRecord(e1, ctx->stream));
+  double *dg = ctx->out.p, *dm = dg + (size_t)ninst * nF * ng, *ds = dm + (size_t)ninst * nF;
+  WL_CHECK(ctx, wl::launch_group_reduce(ctx->partial.p, e.Nl, group, group, ninst, nF, dg, dm, ds,
+                                        ctx->stream));
+  WL_CHECK(ctx, cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (device_ms) *device_ms = ms;
+  ctx->last_launches = ninst + 1;
+  ctx->last_kind = "plain-per-instance";
+  if (out_group)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_group, dg, sizeof(double) * ninst * nF * ng,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  if (out_mean)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_mean, dm, sizeof(double) * ninst * nF,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+  if (out_sem)
+    WL_CHECK(ctx, cudaMemcpyAsync(out_sem, ds, sizeof(double) * ninst * nF,
                                   cudaMemcpyDeviceToHost, ctx->stream));
   return check_status(ctx);
 }

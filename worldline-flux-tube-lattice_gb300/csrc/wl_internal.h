@@ -42,7 +42,31 @@ struct SweepArgs {
   double *partial;   // [n_chunks][nF][3][ninst]
   int *status;       // kDevOk / kDevTimeout
   uint32_t wait_tries;
+  int kprof, fermion, nint;  // kernel selection inside the persistent batch kernel
 };
+
+// Persistent multi-job sweep: a queue of tiles (job, instance tile, loop
+// chunk) drained by one CTA per slot; jobs differ in ensemble, profile,
+// instances, flux values and loops per tile.
+struct BatchTile {
+  int job, tile_x, chunk, cost;
+};
+struct ReduceJob {  // per job: where its partial sums and outputs live
+  const double *partial;
+  double *out_group, *out_mean, *out_sem;
+  int n_chunks, cpg, lpg, ninst, nF, first;  // first: flat (instance, F) index
+};
+struct BatchArgs {
+  const SweepArgs *jobs;
+  const BatchTile *tiles;
+  int ntiles;
+  int *counter;  // next tile to take
+};
+cudaError_t launch_batch(const BatchArgs &a, int grid, cudaStream_t s);
+cudaError_t launch_batch_reduce(const ReduceJob *jobs, int njobs, int total, cudaStream_t s);
+// largest number of batch-kernel CTAs resident per SM
+int batch_max_ctas_per_sm();
+bool batch_supports(int kprof, int nint);
 
 // Loop-parallel sweep: one warp per (loop, instance), lanes over groups of
 // four points; per-loop results.  Used for few instances and for EV().
@@ -61,6 +85,10 @@ struct LoopArgs {
   float4 *scal;     // optional [ninst][Nl] Wsscal of F[0]
   float4 *ferm;     // optional [ninst][Nl] Wsferm of F[0]
 };
+
+// plain per-instance kernel (the batching baseline), light profiles only
+cudaError_t launch_plain(int kprof, bool fermion, int nint, const LoopArgs &a, int inst,
+                         cudaStream_t st);
 
 // returns cudaErrorInvalidValue for an unsupported (profile, nint)
 cudaError_t launch_sweep(int profile, bool fermion, int nint, const SweepArgs &a,

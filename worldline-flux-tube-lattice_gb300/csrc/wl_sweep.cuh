@@ -25,37 +25,46 @@
 
 namespace wl {
 
-template <int P, bool FERM, int NINT>
-__global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweepMinBlocks)
-    sweep_kernel(const __grid_constant__ SweepArgs A) {
-  extern __shared__ __align__(128) float4 ring[];  // [kSweepStages][kSweepChunkPts]
-  __shared__ __align__(8) uint64_t full_bar[kSweepStages];
-  __shared__ int sm_bad;
-  // FP64 W-factor sums per (flux value, factor, instance): kept in shared
-  // memory (touched once per loop) so they do not hold 24 registers
-  __shared__ double sacc[kMaxF * 3][kSweepThreads];
+// Shared-memory state of the sweep, reused by consecutive tiles of a CTA.
+struct SweepShared {
+  uint64_t *full_bar;                  // [kSweepStages] mbarriers
+  double (*sacc)[kSweepThreads];       // [kMaxF * 3][kSweepThreads] FP64 W - 1 sums
+  int *bad;                            // a stage copy timed out
+  float4 *ring;                        // [kSweepStages][kSweepChunkPts]
+};
 
+__device__ __forceinline__ void sweep_shared_init(const SweepShared &S) {
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kSweepStages; ++st) mbar_init(&S.full_bar[st], 1);
+    fence_mbar_init();
+    *S.bad = 0;
+  }
+  __syncthreads();
+}
+
+// One tile: instances [tile_x * kSweepThreads, +kSweepThreads) of A over the
+// loops of chunk `chunk`.  `consumed` counts the stage copies this CTA has
+// waited for before (the ring's barrier phases continue across tiles).
+// Returns false if a copy timed out (status set, nothing written).
+template <int P, bool FERM, int NINT>
+__device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int chunk,
+                                           const SweepShared &S, int &consumed) {
   const int tid = threadIdx.x;
-  const int inst = blockIdx.x * kSweepThreads + tid;
+  const int inst = tile_x * kSweepThreads + tid;
   const int ic = inst < A.ninst ? inst : A.ninst - 1;
-  const int chunk = blockIdx.y;
   const int l0 = chunk * A.chunk_loops;
   const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
   const int K = A.chunk_loops * nck;
+  float4 *const ring = S.ring;
+  uint64_t *const full_bar = S.full_bar;
 
   const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic];
   const FieldDev &F = A.field;
   const df tq = {A.tqh[ic], A.tql[ic]};
+  const int base = consumed;
 
-  if (tid == 0) {
-    for (int st = 0; st < kSweepStages; ++st) mbar_init(&full_bar[st], 1);
-    fence_mbar_init();
-    sm_bad = 0;
-  }
-  __syncthreads();
-
-  auto issue = [&](int k) {  // chunk k -> stage k % kSweepStages
-    const int st = k % kSweepStages;
+  auto issue = [&](int k) {  // chunk k -> stage (base + k) % kSweepStages
+    const int st = (base + k) % kSweepStages;
     const int l = l0 + k / nck, c = k % nck;
     const int p0 = c * kSweepChunkPts;
     const int np = min(kSweepChunkPts, A.ppl - p0);
@@ -68,7 +77,7 @@ __global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweep
     for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
 
 #pragma unroll
-  for (int r = 0; r < kMaxF * 3; ++r) sacc[r][tid] = 0.0;
+  for (int r = 0; r < kMaxF * 3; ++r) S.sacc[r][tid] = 0.0;
 
   // running sums of the current loop: phase and spin, each with compensation
   float ph[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
@@ -79,9 +88,9 @@ __global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweep
 
   int k = 0;
   for (; k < K; ++k) {
-    const int st = k % kSweepStages;
-    const uint32_t par = (uint32_t)(k / kSweepStages) & 1u;
-    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) sm_bad = 1;
+    const int st = (base + k) % kSweepStages;
+    const uint32_t par = (uint32_t)((base + k) / kSweepStages) & 1u;
+    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) *S.bad = 1;
 
     const int c = k % nck;
     const int p0 = c * kSweepChunkPts;
@@ -160,34 +169,52 @@ __global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweep
                        fast_two_sum(sp[2], -sc[2])};
       loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
                           [&](int j, double w0, double w1, double w2) {
-                            sacc[3 * j][tid] += w0;
-                            sacc[3 * j + 1][tid] += w1;
-                            sacc[3 * j + 2][tid] += w2;
+                            S.sacc[3 * j][tid] += w0;
+                            S.sacc[3 * j + 1][tid] += w1;
+                            S.sacc[3 * j + 2][tid] += w2;
                           });
     }
 
     __syncthreads();  // every thread is done with stage st
-    if (sm_bad) break;
+    if (*S.bad) break;
     if (tid == 0 && k + kSweepStages < K) issue(k + kSweepStages);
   }
 
-  if (sm_bad) {
+  if (*S.bad) {
     // a copy did not arrive in time: wait (bounded) for the copies still in
     // flight so that none lands after the CTA exits, report, write nothing
     if (tid == 0) {
       const int kend = min(K, k + kSweepStages);
       for (int kk = k; kk < kend; ++kk)
-        mbar_wait_bounded(&full_bar[kk % kSweepStages], (uint32_t)(kk / kSweepStages) & 1u,
-                          A.wait_tries);
+        mbar_wait_bounded(&full_bar[(base + kk) % kSweepStages],
+                          (uint32_t)((base + kk) / kSweepStages) & 1u, A.wait_tries);
       atomicExch(A.status, kDevTimeout);
     }
-    return;
+    consumed = base + K;
+    return false;
   }
+  consumed = base + K;
 
   if (inst < A.ninst) {
     for (int r = 0; r < A.nF * 3; ++r)
-      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + inst] = sacc[r][tid];
+      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + inst] = S.sacc[r][tid];
   }
+  return true;
+}
+
+template <int P, bool FERM, int NINT>
+__global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweepMinBlocks)
+    sweep_kernel(const __grid_constant__ SweepArgs A) {
+  extern __shared__ __align__(128) float4 ring[];  // [kSweepStages][kSweepChunkPts]
+  __shared__ __align__(8) uint64_t full_bar[kSweepStages];
+  __shared__ int sm_bad;
+  // FP64 W-factor sums per (flux value, factor, instance): kept in shared
+  // memory (touched once per loop) so they do not hold 24 registers
+  __shared__ double sacc[kMaxF * 3][kSweepThreads];
+  const SweepShared S = {full_bar, sacc, &sm_bad, ring};
+  sweep_shared_init(S);
+  int consumed = 0;
+  sweep_tile<P, FERM, NINT>(A, blockIdx.x, blockIdx.y, S, consumed);
 }
 
 template <int P, bool FERM, int NINT>

@@ -48,6 +48,15 @@ def field(profile="smooth", fermion=0, nint=50, mode=MODE_REFCOMPAT, lambda2=1.0
                  float(lambda2), float(tubedist), float(lmin))
 
 
+class Job(C.Structure):
+    """wl_job of wlgpu.h."""
+    _fields_ = [("handle", C.c_int), ("field", Field), ("ninst", C.c_int),
+                ("cx", C.POINTER(C.c_double)), ("cy", C.POINTER(C.c_double)),
+                ("T", C.POINTER(C.c_double)), ("nF", C.c_int), ("F", C.c_double * 4),
+                ("group", C.c_int), ("out_group", C.POINTER(C.c_double)),
+                ("out_mean", C.POINTER(C.c_double)), ("out_sem", C.POINTER(C.c_double))]
+
+
 class Float4(C.Structure):
     _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("w", C.c_float)]
 
@@ -98,6 +107,11 @@ def lib():
         L.wl_tint.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, C.c_int, dp, C.c_int, dp,
                               C.c_int, C.c_int, dp, dp, dp]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
+        L.wl_batch_eval.argtypes = [vp, C.c_int, C.POINTER(Job), C.c_int]
+        L.wl_batch_autotune.argtypes = [vp, C.c_int, C.POINTER(Job), ip, ip]
+        L.wl_batch_stats.argtypes = [vp, dp, ip, ip, ip]
+        L.wl_eval_plain.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, dp, dp, C.c_int,
+                                    dp, C.c_int, dp, dp, dp, dp]
         L.wl_eval_noalloc.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Field), C.c_int, vp, vp,
                                       vp, C.c_int, dp, C.c_int, vp, vp, vp, vp]
         L.wl_loops.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_double,
@@ -228,6 +242,70 @@ class Context:
                                   nbins, _p(leff, C.c_double), _p(err, C.c_double),
                                   _p(ig, C.c_double) if want_igrand else None))
         return leff, err, ig
+
+    def _jobs(self, jobs):
+        """Pack job dicts (handle, field, cx, cy, T, F, group) into wl_job
+        structs with freshly allocated outputs; returns (array, outputs, keep)."""
+        arr = (Job * len(jobs))()
+        outs, keep = [], []
+        for i, j in enumerate(jobs):
+            cx, cy, T, F = _d(j["cx"]), _d(j["cy"]), _d(j["T"]), _d(j["F"])
+            group = j.get("group", 128)
+            Nl = C.c_int()
+            self._check(lib().wl_ensemble_info(self._h, j["handle"], None, C.byref(Nl), None))
+            ng = Nl.value // group
+            g = np.empty((len(T), len(F), max(ng, 1)))
+            m = np.empty((len(T), len(F)))
+            se = np.empty((len(T), len(F)))
+            a = arr[i]
+            a.handle, a.field, a.ninst = j["handle"], j["field"], len(T)
+            a.cx, a.cy, a.T = _p(cx, C.c_double), _p(cy, C.c_double), _p(T, C.c_double)
+            a.nF = len(F)
+            for k, f in enumerate(F):
+                a.F[k] = f
+            a.group = group
+            a.out_group, a.out_mean, a.out_sem = (_p(g, C.c_double), _p(m, C.c_double),
+                                                  _p(se, C.c_double))
+            outs.append((g, m, se))
+            keep += [cx, cy, T, F]
+        return arr, outs, keep
+
+    def batch_eval(self, jobs, graph: bool = True):
+        """Evaluate a list of job dicts in one persistent launch (wl_batch_eval);
+        returns [(groups, mean, sem)] per job."""
+        arr, outs, keep = self._jobs(jobs)
+        self._check(lib().wl_batch_eval(self._h, len(jobs), arr, 1 if graph else 0))
+        return outs
+
+    def batch_autotune(self, jobs):
+        arr, _, keep = self._jobs(jobs)
+        p, c = C.c_int(), C.c_int()
+        self._check(lib().wl_batch_autotune(self._h, len(jobs), arr, C.byref(p), C.byref(c)))
+        return p.value, c.value
+
+    def batch_stats(self):
+        ms, nt, g, p = C.c_double(), C.c_int(), C.c_int(), C.c_int()
+        self._check(lib().wl_batch_stats(self._h, C.byref(ms), C.byref(nt), C.byref(g),
+                                         C.byref(p)))
+        return {"device_ms": ms.value, "tiles": nt.value, "grid": g.value,
+                "points_per_tile": p.value}
+
+    def eval_plain(self, handle: int, fld: Field, cx, cy, T, F, group: int = 128):
+        """The plain per-instance kernel (one launch per instance); returns
+        (groups, mean, sem, device_ms)."""
+        cx, cy, T, F = _d(cx), _d(cy), _d(T), _d(F)
+        Nl = C.c_int()
+        self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), None))
+        ng = Nl.value // group
+        g = np.empty((len(T), len(F), ng))
+        m = np.empty((len(T), len(F)))
+        se = np.empty((len(T), len(F)))
+        ms = C.c_double()
+        self._check(lib().wl_eval_plain(self._h, handle, C.byref(fld), len(T), _p(cx, C.c_double),
+                                        _p(cy, C.c_double), _p(T, C.c_double), len(F),
+                                        _p(F, C.c_double), group, _p(g, C.c_double),
+                                        _p(m, C.c_double), _p(se, C.c_double), C.byref(ms)))
+        return g, m, se, ms.value
 
     def peak_probe(self, kind: int) -> float:
         """Lane operations per second of the FP32 FMA (0) or MUFU rcp (1) pipe."""
