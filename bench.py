@@ -210,6 +210,80 @@ def config_dict():
             "l2": "inputs larger than L2 (160 MiB ensemble), no flush"}
 
 
+def c4_jobs(wltube, ctx, njobs, seed=4, profiles=("smooth", "gaussian")):
+    """Jobs drawn as the uneven-batch configuration: profile, F log-uniform in
+    [0.01, 10], lambda log-uniform in [0.1, 10], ppl in {512..8192}, Nl in
+    {1024..8192}, T count in [16, 256] (log-spaced in [1e-2, 1e2]), rho count in
+    [4, 64] (uniform in [0, 5 lambda]); ensembles keyed by (ppl, Nl, seed)."""
+    rng = np.random.default_rng(seed)
+    ens, jobs = {}, []
+    for _ in range(njobs):
+        prof = profiles[rng.integers(len(profiles))]
+        F = float(np.exp(rng.uniform(np.log(0.01), np.log(10.0))))
+        lam = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
+        ppl = int(rng.choice([512, 1024, 2048, 4096, 8192]))
+        Nl = int(rng.choice([1024, 2048, 4096, 8192]))
+        nT = int(rng.integers(16, 257))
+        nrho = int(rng.integers(4, 65))
+        key = (ppl, Nl)
+        if key not in ens:
+            ens[key] = ctx.generate(seed, Nl, ppl)
+        T = np.geomspace(1e-2, 1e2, nT)
+        rho = np.linspace(0.0, 5.0 * lam, nrho)
+        jobs.append({"handle": ens[key], "field": wltube.field(prof, fermion=1, nint=NINT,
+                                                               lambda2=lam * lam),
+                     "cx": np.repeat(rho, nT), "cy": np.zeros(nrho * nT),
+                     "T": np.tile(T, nrho), "F": [F], "group": 128,
+                     "segments": Nl * ppl * nT * nrho})
+    return jobs, ens
+
+
+def run_batch(args):
+    """Uneven batch in one persistent graph-captured launch vs the plain
+    per-instance kernel (one launch per instance) on a sample."""
+    import wltube
+
+    ctx = wltube.Context(0)
+    jobs, ens = c4_jobs(wltube, ctx, args.jobs)
+    total = sum(j["segments"] for j in jobs)
+    # autotune on a sample: the first jobs with every 8th instance
+    sample = [dict(j, cx=j["cx"][::8], cy=j["cy"][::8], T=j["T"][::8]) for j in jobs[:8]]
+    pts, ctas = ctx.batch_autotune(sample)
+    for _ in range(args.warmup):
+        ctx.batch_eval(jobs, graph=True)
+    ms = []
+    for _ in range(args.steps):
+        ctx.batch_eval(jobs, graph=True)
+        ms.append(ctx.batch_stats()["device_ms"])
+    st = ctx.batch_stats()
+    batched = total / (np.median(ms) * 1e-3)
+    # plain per-instance kernel on a sample of instances of every job
+    psegs, pms = 0, 0.0
+    for j in jobs:
+        idx = np.linspace(0, len(j["T"]) - 1, 2).astype(int)
+        _, _, _, t = ctx.eval_plain(j["handle"], j["field"], j["cx"][idx], j["cy"][idx],
+                                    j["T"][idx], j["F"], j["group"])
+        L = ctx  # noqa: F841
+        Nl_ppl = j["segments"] // len(j["T"])
+        psegs += Nl_ppl * len(idx)
+        pms += t
+    plain = psegs / (pms * 1e-3)
+    print(json.dumps({
+        "metric": "loop-segments/s (uneven batch, one persistent graph launch)",
+        "value": batched, "unit": "segments/s", "ms_per_step": float(np.median(ms)),
+        "steps": args.steps, "warmup": args.warmup, "jobs": len(jobs),
+        "segments_per_step": int(total), "tiles": st["tiles"], "grid": st["grid"],
+        "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas},
+        "plain_per_instance": {"value": plain, "unit": "segments/s",
+                               "sample_instances": 2 * len(jobs), "device_ms": pms},
+        "speedup_vs_plain": batched / plain,
+        "config": {"workload": "uneven batch drawn as the 512-instance configuration "
+                               "(seed 4), %d jobs, profiles smooth+gaussian, spinor, "
+                               "5 Simpson nodes" % len(jobs),
+                   "ensembles": len(ens)}}))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -221,7 +295,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 128 instances on the full ensemble, no e2e/cpu")
+    ap.add_argument("--workload", default="c2", choices=["c2", "batch"],
+                    help="c2: the headline spinor workload; batch: uneven multi-job batch")
+    ap.add_argument("--jobs", type=int, default=32, help="jobs of the batch workload")
     args = ap.parse_args()
+    if args.workload == "batch":
+        run_batch(args)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
