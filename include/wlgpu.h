@@ -44,6 +44,16 @@ extern "C" {
 #define WL_PROFILE_GAUSSIAN 3
 #define WL_PROFILE_PERIODIC 4
 #define WL_PROFILE_FIXFLUX 6
+/* Square lattice of identical Gaussian flux tubes at R = a(m, n), |R| <=
+ * rimage (no counterpart in the reference, whose "periodic" profile is a
+ * radial shell model, intEV.cu:201-232): every image contributes the
+ * reference's single-tube Gaussian segment integral (intEV.cu:408-459,
+ * 282-284) in coordinates relative to R.  Exact mode only: the reference's
+ * b >= 1e-8 clamp would break the pure-gauge cancellation of distant images.
+ * Images farther than sqrt(30) lambda from the loop's bounding box see
+ * f = 1 - e^-30 along the whole loop and lie outside it (winding 0): their
+ * exact contribution is zero and they are skipped. */
+#define WL_PROFILE_LATTICE 8
 
 /* clamp modes of the segment polynomial */
 #define WL_MODE_REFCOMPAT 0 /* the reference's clamps (intEV.cu:418-422, 439) */
@@ -60,6 +70,7 @@ typedef struct {
   double lambda2; /* lambda^2                                                 */
   double tubedist;/* lattice spacing a (periodic, fixflux)                    */
   double lmin;    /* fixflux minimum width (0.1 a in the reference)           */
+  double rimage;  /* lattice: image tubes with |R| <= rimage (e.g. 12 a)      */
 } wl_field;
 
 typedef struct wl_ctx wl_ctx;

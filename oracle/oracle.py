@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 PROFILES = {"step": 0, "smooth": 1, "quadratic": 2, "gaussian": 3,
-            "periodic": 4, "spline": 5, "fixflux": 6}
+            "periodic": 4, "spline": 5, "fixflux": 6, "lattice": 8}
 REFCOMPAT, EXACT = 0, 1
 QED_M2, QED_E = 1.0, 0.30282212  # Integrand.c:12-14
 
@@ -28,7 +28,7 @@ class Field(C.Structure):
     _fields_ = [("profile", C.c_int), ("fermion", C.c_int), ("nint", C.c_int),
                 ("mode", C.c_int), ("ff_variant", C.c_int), ("pad_", C.c_int),
                 ("lambda2", C.c_double), ("tubedist", C.c_double),
-                ("lmin", C.c_double)]
+                ("lmin", C.c_double), ("rimage", C.c_double)]
 
 
 class Qed(C.Structure):
@@ -36,12 +36,14 @@ class Qed(C.Structure):
 
 
 def field(profile="smooth", fermion=0, nint=50, mode=REFCOMPAT, lambda2=1.0,
-          tubedist=1.0, lmin=None, ff_variant=0) -> Field:
+          tubedist=1.0, lmin=None, ff_variant=0, rimage=None) -> Field:
     if isinstance(profile, str):
         profile = PROFILES[profile]
     if lmin is None:
         lmin = 0.1 * tubedist
-    return Field(profile, fermion, nint, mode, ff_variant, 0, lambda2, tubedist, lmin)
+    if rimage is None:
+        rimage = 12.0 * tubedist
+    return Field(profile, fermion, nint, mode, ff_variant, 0, lambda2, tubedist, lmin, rimage)
 
 
 def build(force: bool = False) -> str:

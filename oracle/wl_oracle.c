@@ -74,9 +74,49 @@ void wlo64_idt(double a, double b, double c, const wlo_field *f, double *scalI,
   d_idt(a, b, c, f, scalI, fermI);
 }
 
+/* square lattice of Gaussian tubes (see wl_oracle.h) */
+static void d_lattice_sums(const float *w, int ppl, double cx, double cy, double rtT,
+                           const wlo_field *f, double gs[3], double gf[3]) {
+  wlo_field g = *f;
+  g.profile = WLO_GAUSSIAN;
+  g.mode = WLO_EXACT;
+  const double a = f->tubedist, rcut = WLO_LATTICE_RCUT_L * sqrt(f->lambda2);
+  double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+  for (int i = 0; i < ppl; i++) {
+    double x = cx + rtT * (double)w[4 * i], y = cy + rtT * (double)w[4 * i + 1];
+    xmin = fmin(xmin, x);
+    xmax = fmax(xmax, x);
+    ymin = fmin(ymin, y);
+    ymax = fmax(ymax, y);
+  }
+  const int m0 = (int)ceil((xmin - rcut) / a), m1 = (int)floor((xmax + rcut) / a);
+  const int n0 = (int)ceil((ymin - rcut) / a), n1 = (int)floor((ymax + rcut) / a);
+  const double rr = f->rimage / a;
+  gs[0] = gs[1] = gs[2] = 0;
+  gf[0] = gf[1] = gf[2] = 0;
+  for (int m = m0; m <= m1; m++)
+    for (int n = n0; n <= n1; n++) {
+      if ((double)m * m + (double)n * n > rr * rr * (1.0 + 1e-12)) continue;
+      double s3[3], f3[3];
+      d_loop_sums_impl(w, ppl, cx - m * a, cy - n * a, rtT, &g, s3, f3);
+      for (int k = 0; k < 3; k++) {
+        gs[k] += s3[k];
+        gf[k] += f3[k];
+      }
+    }
+}
+
+static void d_sums(const float *w, int ppl, double cx, double cy, double rtT, const wlo_field *f,
+                   double gs[3], double gf[3]) {
+  if (f->profile == WLO_LATTICE)
+    d_lattice_sums(w, ppl, cx, cy, rtT, f, gs, gf);
+  else
+    d_loop_sums_impl(w, ppl, cx, cy, rtT, f, gs, gf);
+}
+
 void wlo64_loop_sums(const float *loop, int ppl, double cx, double cy, double rtT,
                      const wlo_field *f, double gs[3], double gf[3]) {
-  d_loop_sums_impl(loop, ppl, cx, cy, rtT, f, gs, gf);
+  d_sums(loop, ppl, cx, cy, rtT, f, gs, gf);
 }
 
 void wlo32_loop_sums(const float *loop, int ppl, float cx, float cy, float rtT,
@@ -100,7 +140,7 @@ void wlo64_loops(const float *loops, int Nl, int ppl, double cx, double cy, doub
 #pragma omp parallel for schedule(dynamic, 4)
   for (int l = 0; l < Nl; l++) {
     double gs[3], gf[3];
-    d_loop_sums_impl(loops + (size_t)l * ppl * 4, ppl, cx, cy, rtT, f, gs, gf);
+    d_sums(loops + (size_t)l * ppl * 4, ppl, cx, cy, rtT, f, gs, gf);
     finish_loop(gs, gf, T, F, ppl, scal + 3 * l, ferm + 3 * l);
   }
 }
@@ -177,7 +217,7 @@ static void eval_generic(int fp32, const float *loops, int Nl, int ppl, int nins
           gf[k] = f32[k];
         }
       } else {
-        d_loop_sums_impl(w, ppl, cx[i], cy[i], rtT, f, gs, gf);
+        d_sums(w, ppl, cx[i], cy[i], rtT, f, gs, gf);
       }
       for (int j = 0; j < nF && j < 16; j++) {
         double s[3], fm[3], wv[3];
@@ -262,6 +302,18 @@ double wlo_magfield(double rho2, double F, const wlo_field *f, const wlo_qed *q)
     case WLO_GAUSSIAN: B = rho2 < 100.0 * l2 ? 1.0 / (l2 * exp(rho2 / l2)) : 0.0; break;
     case WLO_PERIODIC: B = d_periodicB(rho2, f); break;
     case WLO_FIXFLUX: B = d_fixfluxB(rho2, f); break;
+    case WLO_LATTICE: {
+      /* no reference: the images' Gaussian fields at (sqrt(rho2), 0) */
+      const double a = f->tubedist, rr = f->rimage / a, x = sqrt(rho2);
+      const int lim = (int)floor(rr);
+      for (int m = -lim; m <= lim; m++)
+        for (int n = -lim; n <= lim; n++) {
+          if ((double)m * m + (double)n * n > rr * rr * (1.0 + 1e-6)) continue;
+          double dx = x - m * a, dy = -n * a, d2 = dx * dx + dy * dy;
+          if (d2 < 40.0 * l2) B += exp(-d2 / l2) / l2;
+        }
+      break;
+    }
     default: B = 0.0;
   }
   return 2.0 * F / q->e * B;
@@ -302,7 +354,8 @@ int wlo_tfunc_regime(double T, double xcmx, double xcmy, double F, const wlo_fie
     case WLO_SMOOTH:
     case WLO_QUADRATIC:
     case WLO_PERIODIC: smallT = 0.5 * (l2 + rho * rho); break;
-    case WLO_GAUSSIAN: smallT = l2; break;
+    case WLO_GAUSSIAN:
+    case WLO_LATTICE: smallT = l2; break;
     case WLO_FIXFLUX:
       smallT = rho * rho < l2 / 4.0 ? 0.25 * l2
                                     : 0.25 * l2 + (rho - sqrt(l2) / 2.0) * (rho - sqrt(l2) / 2.0);

@@ -29,7 +29,9 @@ extern "C" {
 
 /* profile ids: the values of the reconstructed intT.h macros */
 enum { WLO_STEP = 0, WLO_SMOOTH = 1, WLO_QUADRATIC = 2, WLO_GAUSSIAN = 3,
-       WLO_PERIODIC = 4, WLO_SPLINE = 5, WLO_FIXFLUX = 6 };
+       WLO_PERIODIC = 4, WLO_SPLINE = 5, WLO_FIXFLUX = 6,
+       /* square lattice of Gaussian tubes: no reference implementation */
+       WLO_LATTICE = 8 };
 
 /* clamp modes: 0 reproduces the reference clamps (intEV.cu:418-422, 439),
  * 1 evaluates the segment polynomial exactly (only a 1e-30 floor on rho^2
@@ -46,7 +48,19 @@ typedef struct {
   double lambda2;  /* lambda^2                                                 */
   double tubedist; /* lattice spacing a (periodic, fixflux)                    */
   double lmin;     /* fixflux minimum width (0.1 a in the reference runs)      */
+  double rimage;   /* lattice: images R = a(m, n) with |R| <= rimage            */
 } wlo_field;
+
+/* Square lattice of identical Gaussian flux tubes (WLO_LATTICE).  No
+ * reference implementation: each image tube at R = a(m, n), |R| <= rimage,
+ * contributes the single-tube Gaussian segment integral (intEV.cu:408-459 with
+ * f = 1 - exp(-rho^2/lambda^2), intEV.cu:282-284) in coordinates relative to
+ * R, in exact mode (no clamps: the reference's b >= 1e-8 clamp would break
+ * the pure-gauge cancellation of distant images).  Images farther than
+ * WLO_LATTICE_RCUT_L * lambda from the loop's bounding box see f = 1 (to
+ * e^-30) along the whole loop and lie outside it (winding 0): their exact
+ * contribution is zero and they are skipped.                                */
+#define WLO_LATTICE_RCUT_L 5.477225575051661 /* sqrt(30) */
 
 /* ---- profiles (FP64) -------------------------------------------------- */
 double wlo64_flambda(double rho2, const wlo_field *f);

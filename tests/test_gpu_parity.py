@@ -259,3 +259,26 @@ def test_invalid_arguments_return_status(ctx, wl):
             ctx.upload(np.zeros((4, 6, 4), dtype=np.float32))  # ppl not a multiple of 4
     finally:
         ctx.release(h)
+
+
+@pytest.mark.parametrize("a,l2,fe", [(2.0, 1.0, 1), (5.0, 1.0, 0), (2.0, 0.25, 0)])
+def test_lattice_matches_oracle(ctx, wl, a, l2, fe):
+    """Square lattice of Gaussian tubes (image sum to |R| <= 12a) against the
+    FP64 oracle's image sum on a 4 x 4 grid of centres over one unit cell."""
+    loops = O.vloops(3, 128, 128)
+    g1 = (np.arange(4) + 0.5) * a / 4
+    cx0, cy0 = [v.ravel() for v in np.meshgrid(g1, g1)]
+    T0 = np.array([0.05, 0.5, 2.0, 6.0])
+    cx, cy, T = f32_exact(np.repeat(cx0, 4), np.repeat(cy0, 4), np.tile(T0, 16))
+    fld = wl.field("lattice", fermion=fe, nint=4, lambda2=l2, tubedist=a)
+    h = ctx.upload(loops)
+    try:
+        g, _, _ = ctx.eval(h, fld, cx, cy, T, [1.0])
+        s, f = ctx.loops(h, fld, float(cx[5]), float(cy[5]), float(T[5]), 1.0)
+    finally:
+        ctx.release(h)
+    ofld = O.field("lattice", fermion=fe, nint=4, mode=1, lambda2=l2, tubedist=a)
+    ref, S = O.eval_groups(loops, cx, cy, T, [1.0], ofld, return_scale=True)
+    assert werr(g, ref, S) < W_TOL
+    os_, of = O.loops_phases(loops, cx[5], cy[5], T[5], 1.0, ofld)
+    assert np.abs(s[:, :3] - os_).max() / np.abs(os_).max() < PHASE_TOL

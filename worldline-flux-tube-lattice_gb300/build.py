@@ -25,6 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 SOURCES = ["wl_sweep_smooth.cu", "wl_sweep_simple.cu", "wl_sweep_periodic.cu",
+           "wl_sweep_lattice.cu",
            "wl_sweep_fixflux.cu", "wl_misc.cu", "wl_api.cpp", "wl_noalloc.cu",
            "wl_tint.cu", "wl_batch.cu"]
 

@@ -49,6 +49,7 @@ struct Ensemble {
   float4 *dev = nullptr;
   int Nl = 0, ppl = 0;
   bool owned = false;
+  float4 *bbox = nullptr;  // per-loop bounding boxes, computed on first lattice use
 };
 
 typedef CUresult (*AddressRangeFn)(CUdeviceptr *, size_t *, CUdeviceptr);
@@ -136,8 +137,16 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
   if (!f) return fail(ctx, WL_ERR_INVALID, "field is NULL");
   int p = f->profile;
   if (!(p == WL_PROFILE_STEP || p == WL_PROFILE_SMOOTH || p == WL_PROFILE_QUADRATIC ||
-        p == WL_PROFILE_GAUSSIAN || p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX))
+        p == WL_PROFILE_GAUSSIAN || p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX ||
+        p == WL_PROFILE_LATTICE))
     return fail(ctx, WL_ERR_INVALID, "unsupported profile %d", p);
+  if (p == WL_PROFILE_LATTICE) {
+    if (f->mode != WL_MODE_EXACT)
+      return fail(ctx, WL_ERR_INVALID, "the lattice profile needs WL_MODE_EXACT");
+    if (!(f->tubedist > 0.0) || !isfinite(f->tubedist) || !(f->rimage >= 0.0) ||
+        !isfinite(f->rimage) || f->rimage / f->tubedist > 1000.0)
+      return fail(ctx, WL_ERR_INVALID, "lattice: need tubedist > 0 and 0 <= rimage <= 1000 a");
+  }
   if (f->nint < 2 || f->nint > 64 || f->nint % 2)
     return fail(ctx, WL_ERR_INVALID, "nint must be even in [2, 64], got %d", f->nint);
   if (f->mode != WL_MODE_REFCOMPAT && f->mode != WL_MODE_EXACT)
@@ -150,6 +159,7 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
   if (p == WL_PROFILE_FIXFLUX && !(f->tubedist > f->lmin))
     return fail(ctx, WL_ERR_INVALID, "fixflux needs tubedist > lmin");
   *kprofile = (p == WL_PROFILE_FIXFLUX && f->ff_variant) ? wl::kFixfluxFF : p;
+  if (p == WL_PROFILE_LATTICE) *kprofile = wl::kLattice;
   memset(d, 0, sizeof(*d));
   d->l2 = (float)f->lambda2;
   d->inv_l2 = 1.0f / d->l2;
@@ -162,6 +172,11 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
   }
   d->nint = f->nint;
   d->h = 1.0f / (float)f->nint;
+  if (p == WL_PROFILE_LATTICE) {
+    const double rr = f->rimage / f->tubedist;
+    d->rimg2 = (float)(rr * rr * (1.0 + 1e-6));
+    d->rcut = (float)(5.477225575051661 * sqrt(f->lambda2));  // sqrt(30) lambda
+  }
   if (f->mode == WL_MODE_REFCOMPAT) {
     d->clampA = d->clampB = d->clampC = d->clampE = 1.0e-8f;
     d->clampI = 1.0e-10f;
@@ -185,7 +200,8 @@ void fill_flux(Args &a, const wl_field *f, int nF, const double *F) {
   switch (f->profile) {
     case WL_PROFILE_SMOOTH: fs = (double)(float)f->lambda2; break;
     case WL_PROFILE_STEP:
-    case WL_PROFILE_GAUSSIAN: fs = 1.0 / (double)(float)f->lambda2; break;
+    case WL_PROFILE_GAUSSIAN:
+    case WL_PROFILE_LATTICE: fs = 1.0 / (double)(float)f->lambda2; break;
     case WL_PROFILE_QUADRATIC: fs = 2.0 / (double)(float)f->lambda2; break;
     default: fs = 1.0;
   }
@@ -209,6 +225,23 @@ int lookup(wl_ctx *ctx, int handle, Ensemble *e) {
 
 int set_device(wl_ctx *ctx) {
   WL_CHECK(ctx, cudaSetDevice(ctx->device));
+  return WL_OK;
+}
+
+// per-loop bounding boxes of an ensemble, computed once (lattice images)
+int ensure_bbox(wl_ctx *ctx, int handle, const float4 **out) {
+  auto it = ctx->ens.find(handle);
+  if (it == ctx->ens.end()) return fail(ctx, WL_ERR_NOTFOUND, "unknown ensemble %d", handle);
+  Ensemble &e = it->second;
+  if (!e.bbox) {
+    if (cudaMalloc((void **)&e.bbox, sizeof(float4) * e.Nl) != cudaSuccess) {
+      cudaGetLastError();
+      e.bbox = nullptr;
+      return fail(ctx, WL_ERR_NOMEM, "cannot allocate loop bounding boxes");
+    }
+    WL_CHECK(ctx, wl::launch_loop_bbox(e.dev, e.Nl, e.ppl, e.bbox, ctx->stream));
+  }
+  *out = e.bbox;
   return WL_OK;
 }
 
@@ -381,6 +414,10 @@ int batch_plan(wl_ctx *ctx, int njobs, const wl_job *jobs, int points, BatchPlan
     a.kprof = kprofs[i];
     a.fermion = J.field.fermion != 0;
     a.nint = J.field.nint;
+    if (kprofs[i] == wl::kLattice) {
+      int rb = ensure_bbox(ctx, J.handle, &a.bbox);
+      if (rb) return rb;
+    }
     wl::ReduceJob &rj = P->rjobs[i];
     rj.n_chunks = a.n_chunks;
     rj.cpg = J.group / lcs[i];
@@ -580,8 +617,10 @@ int wl_ctx_destroy(wl_ctx *ctx) {
   if (!ctx) return WL_ERR_INVALID;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (auto &kv : ctx->ens)
+  for (auto &kv : ctx->ens) {
     if (kv.second.owned) cudaFree(kv.second.dev);
+    if (kv.second.bbox) cudaFree(kv.second.bbox);
+  }
   ctx->inst.release();
   ctx->partial.release();
   ctx->out.release();
@@ -710,6 +749,7 @@ int wl_ensemble_release(wl_ctx *ctx, int handle) {
   if ((r = set_device(ctx))) return r;
   WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));
   if (e.owned) cudaFree(e.dev);
+  if (e.bbox) cudaFree(e.bbox);
   ctx->ens.erase(handle);
   return WL_OK;
 }
@@ -746,8 +786,8 @@ static int eval_prologue(wl_ctx *ctx, int handle, const wl_field *field, int nin
 // ctx->inst as [cx | cy | rtT | tq].  Outputs are device pointers (may be
 // NULL).  Returns after enqueueing.
 static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &fd,
-                    const wl_field *field, int ninst, int nF, const double *host_F, int group,
-                    double *dg, double *dm, double *ds) {
+                    const float4 *bbox, const wl_field *field, int ninst, int nF,
+                    const double *host_F, int group, double *dg, double *dm, double *ds) {
   const bool fermion = field->fermion != 0;
   const int nint = field->nint;
   const bool use_sweep = ninst >= 32;
@@ -788,6 +828,7 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
     a.partial = ctx->partial.p;
     a.status = ctx->status.p;
     a.wait_tries = 1u << 22;
+    a.bbox = bbox;
     WL_CHECK(ctx, wl::launch_sweep(kprof, fermion, nint, a, ctx->stream));
     ctx->last_kind = "instance-parallel";
   } else {
@@ -806,6 +847,7 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
     fill_flux(a, field, nF, host_F);
     a.field = fd;
     a.partial = ctx->partial.p;
+    a.bbox = bbox;
     WL_CHECK(ctx, wl::launch_loopwarp(kprof, fermion, nint, a, ctx->stream));
     ctx->last_kind = "loop-parallel";
   }
@@ -833,7 +875,9 @@ int wl_eval(wl_ctx *ctx, int handle, const wl_field *field, int ninst, const dou
     return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu outputs", nout);
   }
   double *dg = ctx->out.p, *dm = dg + (size_t)ninst * nF * ng, *ds = dm + (size_t)ninst * nF;
-  if ((r = run_eval(ctx, e, kprof, fd, field, ninst, nF, host_F, group, dg, dm, ds)))
+  const float4 *bb = nullptr;
+  if (kprof == wl::kLattice && (r = ensure_bbox(ctx, handle, &bb))) return r;
+  if ((r = run_eval(ctx, e, kprof, fd, bb, field, ninst, nF, host_F, group, dg, dm, ds)))
     return r;
   ctx->last_launches = 2;
   if (out_group)
@@ -874,7 +918,9 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
   WL_CHECK(ctx, ctx->inst.reserve((size_t)wl::kInstArrays * ninst));
   WL_CHECK(ctx, wl::launch_instance_setup(dev_cx, dev_cy, dev_T, ninst, e.ppl, ctx->inst.p,
                                           ctx->status.p, ctx->stream));
-  if ((r = run_eval(ctx, e, kprof, fd, field, ninst, nF, host_F, group, dev_out_group,
+  const float4 *bb = nullptr;
+  if (kprof == wl::kLattice && (r = ensure_bbox(ctx, handle, &bb))) return r;
+  if ((r = run_eval(ctx, e, kprof, fd, bb, field, ninst, nF, host_F, group, dev_out_group,
                     dev_out_mean, dev_out_sem)))
     return r;
   ctx->last_launches = 3;
@@ -973,7 +1019,10 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
     return fail(ctx, WL_ERR_NOMEM, "cannot allocate %zu outputs", nout);
   }
   double *dg = ctx->out.p;
-  if ((r = run_eval(ctx, e, kprof, fd, field, ninst, nF, host_F, group, dg, nullptr, nullptr)))
+  const float4 *bb = nullptr;
+  if (kprof == wl::kLattice && (r = ensure_bbox(ctx, handle, &bb))) return r;
+  if ((r = run_eval(ctx, e, kprof, fd, bb, field, ninst, nF, host_F, group, dg, nullptr,
+                    nullptr)))
     return r;
   // aux: rho | T | w | F | Ig | leff | err | igrand
   const size_t n_ig = (size_t)nrho * nF * ng, n_le = (size_t)nrho * nF;
@@ -1012,6 +1061,8 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
   ta.l2 = field->lambda2;
   ta.a = field->tubedist;
   ta.lmin = field->lmin;
+  ta.rimg2 = field->tubedist > 0.0 ? (field->rimage / field->tubedist) *
+                                          (field->rimage / field->tubedist) : 0.0;
   ta.m2 = 1.0;         // Integrand.c:12
   ta.e = 0.30282212;   // Integrand.c:14
   WL_CHECK(ctx, wl::launch_tint(ta, ctx->stream));
@@ -1082,7 +1133,7 @@ int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst, con
   FieldDev fd;
   int r = eval_prologue(ctx, handle, field, ninst, nF, host_F, group, &e, &kprof, &fd);
   if (r) return r;
-  if (!wl::batch_supports(kprof, field->nint))
+  if (!wl::plain_supports(kprof))
     return fail(ctx, WL_ERR_INVALID, "the plain kernel covers the step, smooth, quadratic and "
                                      "gaussian profiles");
   if ((r = upload_instances(ctx, ninst, host_cx, host_cy, host_T, e.ppl))) return r;
@@ -1179,6 +1230,7 @@ int wl_loops(wl_ctx *ctx, int handle, const wl_field *field, double cx, double c
   fill_flux(a, field, 1, &F);
   a.field = fd;
   a.partial = ctx->partial.p;
+  if (kprof == wl::kLattice && (r = ensure_bbox(ctx, handle, &a.bbox))) return r;
   a.scal = ds;
   a.ferm = df;
   WL_CHECK(ctx, wl::launch_loopwarp(kprof, field->fermion != 0, field->nint, a, ctx->stream));
@@ -1344,6 +1396,8 @@ double EV(double T, void *p, int *WLlist) {
 // same field validation, flux constants and loop partition as wl_eval_device.
 namespace wl {
 int shared_field_to_dev(const wl_field *f, int *kprofile, FieldDev *d) {
+  // the lattice needs per-loop bounding boxes the library would allocate
+  if (f && f->profile == WL_PROFILE_LATTICE) return WL_ERR_INVALID;
   return field_to_dev(nullptr, f, kprofile, d);
 }
 void shared_fill_flux(SweepArgs &a, const wl_field *f, int nF, const double *F) {

@@ -22,6 +22,7 @@ __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, 
     case kGaussian: sweep_tile<kGaussian, FERM, NINT>(A, tx, chunk, S, consumed); break;
     case kStep: sweep_tile<kStep, FERM, NINT>(A, tx, chunk, S, consumed); break;
     case kQuadratic: sweep_tile<kQuadratic, FERM, NINT>(A, tx, chunk, S, consumed); break;
+    case kLattice: sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed); break;
     default: break;
   }
 }
@@ -194,6 +195,11 @@ cudaError_t launch_plain(int kprof, bool fermion, int nint, const LoopArgs &a, i
 
 bool batch_supports(int kprof, int nint) {
   (void)nint;
+  return kprof == kSmooth || kprof == kGaussian || kprof == kStep || kprof == kQuadratic ||
+         kprof == kLattice;
+}
+
+bool plain_supports(int kprof) {
   return kprof == kSmooth || kprof == kGaussian || kprof == kStep || kprof == kQuadratic;
 }
 

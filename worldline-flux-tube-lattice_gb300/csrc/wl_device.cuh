@@ -290,6 +290,101 @@ __device__ __forceinline__ void segment(float zix, float ziy, float zjx, float z
   if (FERM) sp += fmaf(4.0f, fo, fmaf(2.0f, fe, f0 + f1));
 }
 
+// ---------------------------------------------------------- lattice --
+// Square lattice of Gaussian tubes at R = a(m, n).  Per (loop, instance) the
+// images within rcut of the loop's scaled bounding box (and |R| <= rimage)
+// are summed; farther images are pure gauge outside the loop and contribute 0.
+template <>
+struct Profile<kLattice> {  // spin integrand f' = e^{-x}/l2, x = rho^2/l2
+  static __device__ __forceinline__ float fp_scale(const FieldDev &F) { return F.inv_l2; }
+  static constexpr bool kHeavy = false;
+};
+
+struct ImgRange {
+  int m0, m1, n0, n1;
+};
+
+__device__ __forceinline__ ImgRange image_range(float4 bb, float s, float cx, float cy,
+                                                const FieldDev &F) {
+  const float inva = 1.0f / F.a;
+  const int lim = (int)floorf(sqrtf(F.rimg2));
+  ImgRange r;
+  r.m0 = max(-lim, (int)ceilf((fmaf(s, bb.x, cx) - F.rcut) * inva));
+  r.m1 = min(lim, (int)floorf((fmaf(s, bb.y, cx) + F.rcut) * inva));
+  r.n0 = max(-lim, (int)ceilf((fmaf(s, bb.z, cy) - F.rcut) * inva));
+  r.n1 = min(lim, (int)floorf((fmaf(s, bb.w, cy) + F.rcut) * inva));
+  return r;
+}
+
+// (1 - e^-x)/x and e^-x for x >= 0 (x slightly below 0 from rounding is fine)
+__device__ __forceinline__ void gauss_q(float x, float &q, float &e) {
+  e = expneg_fast(x);
+  const float big = (1.0f - e) * rcp_fast(x);
+  const float small = one_minus_expneg_over_x(x);
+  q = x < 0.5f ? small : big;
+}
+
+// One segment z_i -> z_j against every image of the range: in units of
+// x = rho^2/lambda^2, the reference's Gaussian Simpson integral per image,
+// exact mode (no clamps).  Adds sum_R (u_R x Delta)/l2 * sum_w q(x) to ph and
+// sum_R sum_w e^-x to sp (the f' scale 1/l2 is applied per loop).
+template <bool FERM, int NINT>
+__device__ __forceinline__ void segment_lattice(float zix, float ziy, float zjx, float zjy,
+                                                const FieldDev &F, const ImgRange &img,
+                                                float &ph, float &sp) {
+  const float dx = zjx - zix, dy = zjy - ziy;
+  const float il2 = F.inv_l2;
+  const float cs = fmaf(dx, dx, dy * dy) * il2;
+  const int nint = NINT > 0 ? NINT : F.nint;
+  const float h = NINT > 0 ? 1.0f / (float)NINT : F.h;
+  for (int m = img.m0; m <= img.m1; ++m) {
+    const float ux = fmaf(-(float)m, F.a, zix);
+    const float mm = (float)(m * m);
+    for (int n = img.n0; n <= img.n1; ++n) {
+      if (mm + (float)(n * n) > F.rimg2) continue;
+      const float uy = fmaf(-(float)n, F.a, ziy);
+      const float as = fmaf(ux, ux, uy * uy) * il2;
+      const float bs2 = 2.0f * fmaf(ux, dx, uy * dy) * il2;
+      const float cross = fmaf(ux, dy, -(uy * dx)) * il2;  // (z_i - R) x (z_j - R) / l2
+      float q0, e0, q1, e1;
+      gauss_q(as, q0, e0);
+      gauss_q((as + bs2) + cs, q1, e1);
+      float so = 0.f, se = 0.f, fo = 0.f, fe = 0.f;
+      auto node = [&](int j, float t) {
+        float q, e;
+        gauss_q(fmaf(fmaf(cs, t, bs2), t, as), q, e);
+        if (j & 1) {
+          so += q;
+          if (FERM) fo += e;
+        } else {
+          se += q;
+          if (FERM) fe += e;
+        }
+      };
+      if constexpr (NINT > 0) {
+#pragma unroll
+        for (int j = 1; j < NINT; j++) node(j, (float)j * (1.0f / (float)NINT));
+      } else {
+#pragma unroll 1
+        for (int j = 1; j < nint; j++) node(j, (float)j * h);
+      }
+      ph = fmaf(cross, fmaf(4.0f, so, fmaf(2.0f, se, q0 + q1)), ph);
+      if (FERM) sp += fmaf(4.0f, fo, fmaf(2.0f, fe, e0 + e1));
+    }
+  }
+}
+
+// the segment of profile P (the image range is used by the lattice only)
+template <int P, bool FERM, int NINT>
+__device__ __forceinline__ void seg(float zix, float ziy, float zjx, float zjy,
+                                    const FieldDev &F, const ImgRange &img, float &ph,
+                                    float &sp) {
+  if constexpr (P == kLattice)
+    segment_lattice<FERM, NINT>(zix, ziy, zjx, zjy, F, img, ph, sp);
+  else
+    segment<P, FERM, NINT>(zix, ziy, zjx, zjy, F, ph, sp);
+}
+
 // Kahan compensated accumulation: sum - comp is the running total.
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
   const float y = x - comp;

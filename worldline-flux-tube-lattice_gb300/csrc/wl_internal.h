@@ -43,6 +43,7 @@ struct SweepArgs {
   int *status;       // kDevOk / kDevTimeout
   uint32_t wait_tries;
   int kprof, fermion, nint;  // kernel selection inside the persistent batch kernel
+  const float4 *bbox;        // lattice: [Nl] unit-loop (xmin, xmax, ymin, ymax)
 };
 
 // Persistent multi-job sweep: a queue of tiles (job, instance tile, loop
@@ -67,6 +68,7 @@ cudaError_t launch_batch_reduce(const ReduceJob *jobs, int njobs, int total, cud
 // largest number of batch-kernel CTAs resident per SM
 int batch_max_ctas_per_sm();
 bool batch_supports(int kprof, int nint);
+bool plain_supports(int kprof);
 
 // Loop-parallel sweep: one warp per (loop, instance), lanes over groups of
 // four points; per-loop results.  Used for few instances and for EV().
@@ -84,6 +86,7 @@ struct LoopArgs {
   double *partial;  // [Nl][nF][3][ninst]  (chunk = one loop)
   float4 *scal;     // optional [ninst][Nl] Wsscal of F[0]
   float4 *ferm;     // optional [ninst][Nl] Wsferm of F[0]
+  const float4 *bbox;  // lattice: [Nl] unit-loop bounding boxes
 };
 
 // plain per-instance kernel (the batching baseline), light profiles only
@@ -127,11 +130,16 @@ struct TintArgs {
   int nrho, nT, nF, ng, nbins;
   int profile, fermion;
   double l2, a, lmin, m2, e;
+  double rimg2;   // lattice: (rimage / a)^2
+  double xcm_x;   // scratch: the centre of mass of the current evaluation
   double *igrand;  // optional [nrho][nF][nT][ng]
   double *Ig;      // [nrho][nF][ng]
   double *leff, *err;  // [nrho][nF]
 };
 cudaError_t launch_tint(const TintArgs &a, cudaStream_t s);
+
+// per-loop bounding boxes of an ensemble (lattice image selection)
+cudaError_t launch_loop_bbox(const float4 *loops, int Nl, int ppl, float4 *out, cudaStream_t s);
 
 // seeded unit loops
 cudaError_t launch_vloops(uint64_t seed, int first, int Nl, int ppl, float4 *out,

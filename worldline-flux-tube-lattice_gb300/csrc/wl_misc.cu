@@ -15,6 +15,8 @@ cudaError_t launch_sweep_periodic(int, bool, int, const SweepArgs *, const LoopA
                                   cudaStream_t);
 cudaError_t launch_sweep_fixflux(int, bool, int, const SweepArgs *, const LoopArgs *,
                                  cudaStream_t);
+cudaError_t launch_sweep_lattice(int, bool, int, const SweepArgs *, const LoopArgs *,
+                                 cudaStream_t);
 
 static cudaError_t dispatch(int profile, bool fermion, int nint, const SweepArgs *sa,
                             const LoopArgs *la, cudaStream_t s) {
@@ -26,6 +28,7 @@ static cudaError_t dispatch(int profile, bool fermion, int nint, const SweepArgs
     case kPeriodic: return launch_sweep_periodic(profile, fermion, nint, sa, la, s);
     case kFixflux:
     case kFixfluxFF: return launch_sweep_fixflux(profile, fermion, nint, sa, la, s);
+    case kLattice: return launch_sweep_lattice(profile, fermion, nint, sa, la, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -156,6 +159,37 @@ cudaError_t launch_instance_setup(const double *cx, const double *cy, const doub
   const int bs = 256;
   instance_setup_kernel<<<(ninst + bs - 1) / bs, bs, 0, s>>>(cx, cy, T, ninst, ppl, out,
                                                              status);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------ bounding boxes --
+// one warp per loop: (xmin, xmax, ymin, ymax) of the unit loop
+__global__ void loop_bbox_kernel(const float4 *__restrict__ loops, int Nl, int ppl,
+                                 float4 *__restrict__ out) {
+  const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (l >= Nl) return;
+  const float4 *w = loops + (size_t)l * ppl;
+  float x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+  for (int p = lane; p < ppl; p += 32) {
+    const float4 v = w[p];
+    x0 = fminf(x0, v.x);
+    x1 = fmaxf(x1, v.x);
+    y0 = fminf(y0, v.y);
+    y1 = fmaxf(y1, v.y);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, off));
+    x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, off));
+    y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, off));
+    y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, off));
+  }
+  if (lane == 0) out[l] = make_float4(x0, x1, y0, y1);
+}
+
+cudaError_t launch_loop_bbox(const float4 *loops, int Nl, int ppl, float4 *out, cudaStream_t s) {
+  const int warps = 4;
+  loop_bbox_kernel<<<(Nl + warps - 1) / warps, warps * 32, 0, s>>>(loops, Nl, ppl, out);
   return cudaGetLastError();
 }
 

@@ -85,6 +85,7 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
   // previous point of each sub-loop and the first points (closing segments)
   float zAx = 0.f, zAy = 0.f, zBx = 0.f, zBy = 0.f, zOx = 0.f, zOy = 0.f;
   float z0x = 0.f, z0y = 0.f, z1x = 0.f, z1y = 0.f, z2x = 0.f, z2y = 0.f;
+  ImgRange img = {0, -1, 0, -1};  // lattice images of the current loop
 
   int k = 0;
   for (; k < K; ++k) {
@@ -107,12 +108,13 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
     if (c == 0) {  // first chunk of a loop: points 0..3 open the sub-loops
 #pragma unroll
       for (int r = 0; r < 3; ++r) ph[r] = pc[r] = sp[r] = sc[r] = 0.f;
+      if constexpr (P == kLattice) img = image_range(A.bbox[l0 + k / nck], s, cx, cy, F);
       float z3x, z3y;
       pt(0, z0x, z0y);
       pt(1, z1x, z1y);
       pt(2, z2x, z2y);
       pt(3, z3x, z3y);
-      segment<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, ph[0], sp[0]);  // N/2: 1 -> 3
+      seg<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, img, ph[0], sp[0]);  // N/2: 1 -> 3
       zAx = z0x; zAy = z0y;
       zBx = z2x; zBy = z2y;
       zOx = z3x; zOy = z3y;
@@ -127,10 +129,10 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
         pt(4 * qq + 1, P1x, P1y);
         pt(4 * qq + 2, P2x, P2y);
         pt(4 * qq + 3, P3x, P3y);
-        segment<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, bp2, bs2);  // N/4a: 4q-4 -> 4q
-        segment<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, bp0, bs0);  // N/2 : 4q-1 -> 4q+1
-        segment<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, bp1, bs1);  // N/4b: 4q-2 -> 4q+2
-        segment<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, bp0, bs0);  // N/2 : 4q+1 -> 4q+3
+        seg<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, img, bp2, bs2);  // N/4a: 4q-4 -> 4q
+        seg<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, img, bp0, bs0);  // N/2 : 4q-1 -> 4q+1
+        seg<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, img, bp1, bs1);  // N/4b: 4q-2 -> 4q+2
+        seg<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, img, bp0, bs0);  // N/2 : 4q+1 -> 4q+3
         zAx = P0x; zAy = P0y;
         zBx = P2x; zBy = P2y;
         zOx = P3x; zOy = P3y;
@@ -154,9 +156,9 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
 
     if (c == nck - 1) {  // last chunk: closing segments back to points 1, 0, 2
       float tp0 = 0.f, tp1 = 0.f, tp2 = 0.f, ts0 = 0.f, ts1 = 0.f, ts2 = 0.f;
-      segment<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, tp0, ts0);  // N/2 : N-1 -> 1
-      segment<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, tp1, ts1);  // N/4b: N-2 -> 2
-      segment<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, tp2, ts2);  // N/4a: N-4 -> 0
+      seg<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, img, tp0, ts0);  // N/2 : N-1 -> 1
+      seg<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, img, tp1, ts1);  // N/4b: N-2 -> 2
+      seg<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, img, tp2, ts2);  // N/4a: N-4 -> 0
       kahan_add(ph[0], pc[0], tp0);
       kahan_add(ph[1], pc[1], tp1);
       kahan_add(ph[2], pc[2], tp2);
@@ -235,6 +237,8 @@ __global__ void __launch_bounds__(kLoopWarps * 32)
   // group q covers points 4q..4q+3 and the four segments ending there; the
   // previous points of group 0 wrap to the end of the loop (closing segments)
   const int nq = A.ppl >> 2;
+  ImgRange img = {0, -1, 0, -1};
+  if constexpr (P == kLattice) img = image_range(A.bbox[l], s, cx, cy, F);
   float ph[3] = {0.f, 0.f, 0.f}, sp[3] = {0.f, 0.f, 0.f};
   for (int q = lane; q < nq; q += 32) {
     const int pa = (q == 0 ? A.ppl : 4 * q) - 4;
@@ -246,10 +250,10 @@ __global__ void __launch_bounds__(kLoopWarps * 32)
     pt(4 * q + 1, P1x, P1y);
     pt(4 * q + 2, P2x, P2y);
     pt(4 * q + 3, P3x, P3y);
-    segment<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, ph[2], sp[2]);
-    segment<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, ph[0], sp[0]);
-    segment<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, ph[1], sp[1]);
-    segment<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, ph[0], sp[0]);
+    seg<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, img, ph[2], sp[2]);
+    seg<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, img, ph[0], sp[0]);
+    seg<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, img, ph[1], sp[1]);
+    seg<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, img, ph[0], sp[0]);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -298,6 +302,8 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
   if constexpr (!Profile<P>::kHeavy) {
     WL_SWEEP_CASE(true, 4)
     WL_SWEEP_CASE(false, 4)
+  }
+  if constexpr (!Profile<P>::kHeavy && P != kLattice) {
     WL_SWEEP_CASE(true, 50)
     WL_SWEEP_CASE(false, 50)
   }
@@ -318,6 +324,8 @@ cudaError_t loopwarp_dispatch(bool fermion, int nint, const LoopArgs &a, cudaStr
   if constexpr (!Profile<P>::kHeavy) {
     WL_LOOP_CASE(true, 4)
     WL_LOOP_CASE(false, 4)
+  }
+  if constexpr (!Profile<P>::kHeavy && P != kLattice) {
     WL_LOOP_CASE(true, 50)
     WL_LOOP_CASE(false, 50)
   }

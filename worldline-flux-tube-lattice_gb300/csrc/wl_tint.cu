@@ -55,19 +55,34 @@ __device__ double magfield_d(const TintArgs &A, double rho2, double F) {
       B = 2.0 / (l2 * 0.0742478) * (1.0 - 0.75 * lml) * bump + 3.0 / (a * a) * lml;
       break;
     }
+    case kLattice: {  // sum of the images' Gaussian fields (|R| <= rimage)
+      const double cutoff2 = 40.0 * l2;  // e^-40: beyond, an image adds nothing
+      const int lim = (int)floor(sqrt(A.rimg2));
+      for (int m = -lim; m <= lim; ++m)
+        for (int n = -lim; n <= lim; ++n) {
+          if ((double)(m * m + n * n) > A.rimg2) continue;
+          const double dx = A.xcm_x - m * a, dy = -n * a;
+          const double d2 = dx * dx + dy * dy;
+          if (d2 < cutoff2) B += exp(-d2 / l2) / l2;
+        }
+      (void)rho2;
+      break;
+    }
     default: B = 0.0;
   }
   return 2.0 * F / A.e * B;
 }
 
 // Tfunc's integrand for one group (Integrand.c:215-305)
-__device__ double igrand_d(const TintArgs &A, double rho, double T, double F, double W) {
+__device__ double igrand_d(TintArgs A, double rho, double T, double F, double W) {
   const double rho2 = rho * rho, l2 = A.l2, m2 = A.m2, e = A.e;
+  A.xcm_x = rho;
   const double B = magfield_d(A, rho2, F), TB = e * T * B;
   double smallT;
   switch (A.profile) {
     case kStep: smallT = (double)abs((int)(rho * rho - l2)); break;
-    case kGaussian: smallT = l2; break;
+    case kGaussian:
+    case kLattice: smallT = l2; break;
     case kFixflux:
     case kFixfluxFF:
       smallT = rho2 < l2 / 4.0 ? 0.25 * l2 : 0.25 * l2 + (rho - sqrt(l2) / 2.0) * (rho - sqrt(l2) / 2.0);

@@ -12,7 +12,8 @@ enum : int {
   kGaussian = 3,
   kPeriodic = 4,
   kFixflux = 6,
-  kFixfluxFF = 7  // fixflux with the intEVff.cu phi/chi fits
+  kFixfluxFF = 7,  // fixflux with the intEVff.cu phi/chi fits
+  kLattice = 8     // square lattice of Gaussian tubes (image sum)
 };
 
 constexpr int kMaxF = 4;  // flux values sharing one geometric pass
@@ -27,6 +28,9 @@ struct FieldDev {
   float clampA, clampB, clampC, clampE, clampI;
   int nint;  // Simpson intervals (used by the run-time-n kernels)
   float h;   // 1.0f / nint
+  // lattice: images with m^2 + n^2 <= rimg2 (|R| <= rimage), near-image
+  // margin rcut = sqrt(30) lambda around the loop's bounding box
+  float rimg2, rcut;
 };
 
 }  // namespace wl

@@ -18,7 +18,7 @@ PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "lib", "libwlgpu.so")
 
 PROFILES = {"step": 0, "smooth": 1, "quadratic": 2, "gaussian": 3, "periodic": 4,
-            "fixflux": 6}
+            "fixflux": 6, "lattice": 8}
 MODE_REFCOMPAT, MODE_EXACT = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
           -4: "device wait timed out", -5: "unknown handle", -6: "admission rejected"}
@@ -35,17 +35,24 @@ class Field(C.Structure):
     """wl_field of wlgpu.h."""
     _fields_ = [("profile", C.c_int), ("fermion", C.c_int), ("nint", C.c_int),
                 ("mode", C.c_int), ("ff_variant", C.c_int), ("reserved", C.c_int),
-                ("lambda2", C.c_double), ("tubedist", C.c_double), ("lmin", C.c_double)]
+                ("lambda2", C.c_double), ("tubedist", C.c_double), ("lmin", C.c_double),
+                ("rimage", C.c_double)]
 
 
-def field(profile="smooth", fermion=0, nint=50, mode=MODE_REFCOMPAT, lambda2=1.0,
-          tubedist=1.0, lmin=None, ff_variant=0) -> Field:
+def field(profile="smooth", fermion=0, nint=50, mode=None, lambda2=1.0,
+          tubedist=1.0, lmin=None, ff_variant=0, rimage=None) -> Field:
+    """wl_field; the lattice profile defaults to exact mode and images within
+    12 lattice spacings, the others to the reference's clamps."""
     if isinstance(profile, str):
         profile = PROFILES[profile]
+    if mode is None:
+        mode = MODE_EXACT if profile == PROFILES["lattice"] else MODE_REFCOMPAT
     if lmin is None:
         lmin = 0.1 * tubedist
+    if rimage is None:
+        rimage = 12.0 * tubedist
     return Field(profile, int(fermion), int(nint), int(mode), int(ff_variant), 0,
-                 float(lambda2), float(tubedist), float(lmin))
+                 float(lambda2), float(tubedist), float(lmin), float(rimage))
 
 
 class Job(C.Structure):
