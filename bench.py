@@ -284,6 +284,113 @@ def run_batch(args):
     ctx.close()
 
 
+def c5_requests(wltube, n, seed=5, profiles=("smooth", "gaussian", "lattice")):
+    """Requests drawn as the served-stream configuration (sizes as the uneven
+    batch): profile in {smooth, Gaussian, lattice a = 5 lambda}, spinor, F
+    log-uniform in [0.01, 10], lambda log-uniform in [0.1, 10], ppl in
+    {512..8192}, Nl in {1024..8192}, T count in [16, 256] log-spaced in
+    [1e-2, 1e2], rho count in [4, 64] uniform in [0, 5 lambda]; half <W>
+    requests, half effective-action-density requests (jackknife over 8 bins);
+    ensembles keyed by (seed, Nl, ppl)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        prof = profiles[rng.integers(len(profiles))]
+        F = float(np.exp(rng.uniform(np.log(0.01), np.log(10.0))))
+        lam = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
+        ppl = int(rng.choice([512, 1024, 2048, 4096, 8192]))
+        Nl = int(rng.choice([1024, 2048, 4096, 8192]))
+        nT = int(rng.integers(16, 257))
+        nrho = int(rng.integers(4, 65))
+        kw = {"tubedist": 5.0 * lam} if prof == "lattice" else {}
+        fld = wltube.field(prof, fermion=1, nint=NINT, lambda2=lam * lam, **kw)
+        out.append({"kind": "leff" if rng.random() < 0.5 else "w", "seed": seed, "Nl": Nl,
+                    "ppl": ppl, "field": fld, "F": [F], "rho": np.linspace(0.0, 5.0 * lam, nrho),
+                    "T": np.geomspace(1e-2, 1e2, nT), "segments": Nl * ppl * nT * nrho})
+    return out
+
+
+def serve_phase(wltube, reqs, rate, seed, max_requests):
+    """Poisson arrivals at `rate` req/s into a fresh server whose ensembles
+    were made resident beforehand; returns the server's statistics."""
+    import threading
+
+    srv = wltube.Server(0, max_requests=max_requests)
+    for key in sorted({(r["Nl"], r["ppl"]) for r in reqs}):   # resident ensembles
+        srv.wait(srv.submit_w(reqs[0]["seed"], key[0], key[1], reqs[0]["field"], [0.0],
+                              [0.0], [1.0], [1.0]), -1.0)
+    srv.reset_stats()
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, len(reqs))
+    tickets = []
+
+    def producer():
+        t0 = time.perf_counter()
+        at = 0.0
+        for r, g in zip(reqs, gaps):
+            at += g
+            dt = t0 + at - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            if r["kind"] == "w":
+                n = len(r["rho"]) * len(r["T"])
+                tk = srv.submit_w(r["seed"], r["Nl"], r["ppl"], r["field"],
+                                  np.repeat(r["rho"], len(r["T"])), np.zeros(n),
+                                  np.tile(r["T"], len(r["rho"])), r["F"])
+            else:
+                tk = srv.submit_leff(r["seed"], r["Nl"], r["ppl"], r["field"], r["rho"], r["T"],
+                                     r["F"], nbins=8)
+            tickets.append(tk)
+
+    th = threading.Thread(target=producer)
+    th.start()
+    th.join()
+    for tk in tickets:
+        srv.wait(tk, -1.0)
+    st = srv.stats()
+    srv.close()
+    return st
+
+
+def run_serve(args):
+    """Served stream: an overload phase (Poisson arrivals at the configuration's
+    lowest rate, 200 req/s) measures the sustained throughput; a second phase
+    offers 70% of that rate and reports the latency percentiles."""
+    import wltube
+
+    n = args.requests
+    profiles = tuple(args.serve_profiles.split(","))
+    reqs = c5_requests(wltube, 2 * n, profiles=profiles)
+    phases = []
+    for name, rate, part in (("overload", 200.0, reqs[:n]), ("sustainable", None, reqs[n:])):
+        if rate is None:
+            rate = 0.7 * phases[0]["sustained_req_s"]
+        t0 = time.time()
+        st = serve_phase(wltube, part, rate, 50 + len(phases), args.max_requests)
+        sys.stderr.write("serve phase %s: %.1f s, %s\n" % (name, time.time() - t0, st))
+        wall = st["wall_s"]  # first submit -> last completion of the phase
+        phases.append({"phase": name, "offered_req_s": rate, "requests": len(part),
+                       "completed": st["completed"], "rejected": st["rejected"],
+                       "failed": st["failed"],
+                       "sustained_req_s": st["completed"] / wall if wall > 0 else None,
+                       "segments_per_s": st["segments"] / wall if wall > 0 else None,
+                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "p999_ms": st["p999_ms"],
+                       "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+                       "launches": st["launches"], "resident_ensembles": st["resident_ensembles"]})
+    sus = phases[1]
+    print(json.dumps({
+        "metric": "serve p50/p99 latency and loop-segments/s (continuous batching)",
+        "value": sus["segments_per_s"], "unit": "segments/s",
+        "p50_ms": sus["p50_ms"], "p99_ms": sus["p99_ms"], "p999_ms": sus["p999_ms"],
+        "phases": phases,
+        "config": {"workload": "served stream drawn as the served-stream configuration "
+                               "(seed 5): %d requests per phase, profiles %s, spinor, "
+                               "5 Simpson nodes, half <W> and half effective-action-density "
+                               "requests, ensembles resident before the phase"
+                               % (n, "+".join(profiles)),
+                   "max_requests": args.max_requests, "quantum_ms": 20.0,
+                   "points_per_tile": 16384}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -295,12 +402,22 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 128 instances on the full ensemble, no e2e/cpu")
-    ap.add_argument("--workload", default="c2", choices=["c2", "batch"],
-                    help="c2: the headline spinor workload; batch: uneven multi-job batch")
+    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "serve"],
+                    help="c2: the headline spinor workload; batch: uneven multi-job batch; "
+                         "serve: Poisson request stream through the server")
     ap.add_argument("--jobs", type=int, default=32, help="jobs of the batch workload")
+    ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
+    ap.add_argument("--serve-profiles", default="smooth,gaussian",
+                    help="profiles of the served requests (lattice requests cost up to "
+                         "hundreds of single-tube segments each: one per image)")
+    ap.add_argument("--max-requests", type=int, default=64,
+                    help="requests the server admits at once (serve workload)")
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -236,6 +236,80 @@ int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
                   int nF, const double *host_F, int group, double *out_group,
                   double *out_mean, double *out_sem, double *device_ms);
 
+/* ---- serving: continuously batched requests ----------------------------- */
+#define WL_REQ_W 0    /* <W> per group of every (cx, cy, T) instance            */
+#define WL_REQ_LEFF 1 /* effective action density L_eff(rho) as wl_tint        */
+
+/* One request.  The ensemble is named by (seed, Nl, ppl) and generated on the
+ * device the first time it is needed; it then stays resident.  Input arrays
+ * are copied at submit; output arrays must stay valid until the request
+ * completes. */
+typedef struct {
+  uint64_t seed;
+  int Nl, ppl;
+  wl_field field;
+  int kind;                         /* WL_REQ_W or WL_REQ_LEFF                  */
+  int ninst;                        /* WL_REQ_W: instances                      */
+  const double *cx, *cy, *T;
+  int nrho, nT, nbins;              /* WL_REQ_LEFF: rho x log-spaced T grid     */
+  const double *rho, *Tgrid;
+  int nF;
+  double F[4];
+  int group;
+  double *out_group, *out_mean, *out_sem;  /* WL_REQ_W (layouts as wl_eval)  */
+  double *out_leff, *out_err;              /* WL_REQ_LEFF: [nrho][nF]        */
+} wl_request;
+
+typedef struct {
+  long long submitted, completed, rejected, failed;
+  double p50_ms, p99_ms, p999_ms, mean_ms, max_ms;  /* submit -> complete      */
+  double wall_s;            /* first submit -> last completion                */
+  double segments;          /* loop-segments of the completed requests        */
+  long long launches;       /* persistent-kernel launches                     */
+  int resident_ensembles;
+  double hbm_bytes_in_use;  /* ensembles + admitted requests' buffers         */
+} wl_server_stats;
+
+typedef struct wl_server wl_server;
+
+typedef struct {
+  int device;
+  double hbm_budget_bytes;  /* ensembles + admitted requests; 0: 80% of the
+                               device memory free at creation                 */
+  double quantum_ms;        /* target device time of one launch; 0: 20 ms     */
+  int points_per_tile;      /* loop points per tile; 0: 16384 (the batch
+                               default, so results equal wl_batch_eval's)     */
+  int ctas_per_sm;          /* persistent CTAs per SM; 0: occupancy limit     */
+  int max_requests;         /* requests admitted at once; 0: 1024             */
+} wl_server_config;
+
+/* A request server: a worker thread admits requests in arrival order while
+ * their HBM footprint (buffers, plus the ensemble if it is not resident) fits
+ * the budget, least recently used idle ensembles being evicted when needed;
+ * a request that can never fit completes with WL_ERR_ADMISSION.  Every
+ * admitted request is cut into (instance tile, loop chunk) tiles; each launch
+ * of the persistent kernel takes about quantum_ms of tiles from all admitted
+ * requests, oldest first, and two launches are kept in flight on two streams
+ * so that new requests' work overlaps the tail of the running one.  Results
+ * of a WL_REQ_W request are bit-identical to wl_batch_eval of the request
+ * alone with the same points_per_tile; a WL_REQ_LEFF request integrates
+ * those <W> values over proper time as wl_tint does. */
+int wl_server_create(const wl_server_config *cfg, wl_server **out);
+/* thread-safe; checks and copies the inputs; *ticket names the request */
+int wl_server_submit(wl_server *srv, const wl_request *req, long long *ticket);
+#define WL_PENDING 1 /* wl_server_wait: the request is not done yet        */
+/* waits for a request (timeout_ms < 0: forever): WL_PENDING if it is not done
+ * within timeout_ms, else the request's own status (the ticket is then
+ * forgotten) */
+int wl_server_wait(wl_server *srv, long long ticket, double timeout_ms);
+int wl_server_get_stats(wl_server *srv, wl_server_stats *stats);
+/* clears the statistics (latencies, counters, clocks); resident ensembles stay */
+int wl_server_reset_stats(wl_server *srv);
+/* the last error message of a submit or of the worker */
+int wl_server_last_error(wl_server *srv, char *buf, int buflen);
+/* finishes the admitted and queued requests, stops the worker, frees all */
+int wl_server_destroy(wl_server *srv);
+
 /* ---- legacy EV() configuration ----------------------------------------- */
 /* The reference selects the profile at compile time (intT.h "profile"); the
  * library's EV() uses the profile, lattice spacing, Simpson intervals and

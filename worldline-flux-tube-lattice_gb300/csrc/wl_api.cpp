@@ -1392,6 +1392,8 @@ double EV(double T, void *p, int *WLlist) {
 }  // extern "C"
 #pragma GCC visibility pop
 
+static void log_simpson_weights(const double *T, int n, double du, double *w);
+
 // Helpers shared with the allocation-free entry point (wl_noalloc.cu): the
 // same field validation, flux constants and loop partition as wl_eval_device.
 namespace wl {
@@ -1407,4 +1409,18 @@ void shared_fill_flux(LoopArgs &a, const wl_field *f, int nF, const double *F) {
   fill_flux(a, f, nF, F);
 }
 int shared_plan_chunk(int group) { return plan_chunk(group); }
+
+// for the request server (wl_server.cpp)
+int rt_field(const wl_field *f, int *kprofile, FieldDev *d, std::string *err) {
+  wl_ctx tmp;
+  const int r = field_to_dev(&tmp, f, kprofile, d);
+  if (r && err) *err = tmp.err;
+  return r;
+}
+int rt_loops_per_tile(int points, int ppl, int group) {
+  return batch_loops_per_tile(points, ppl, group);
+}
+void rt_log_simpson_weights(const double *T, int n, double du, double *w) {
+  log_simpson_weights(T, n, du, w);
+}
 }  // namespace wl

@@ -64,6 +64,39 @@ class Job(C.Structure):
                 ("out_mean", C.POINTER(C.c_double)), ("out_sem", C.POINTER(C.c_double))]
 
 
+class Request(C.Structure):
+    """wl_request of wlgpu.h."""
+    _fields_ = [("seed", C.c_uint64), ("Nl", C.c_int), ("ppl", C.c_int), ("field", Field),
+                ("kind", C.c_int), ("ninst", C.c_int),
+                ("cx", C.POINTER(C.c_double)), ("cy", C.POINTER(C.c_double)),
+                ("T", C.POINTER(C.c_double)), ("nrho", C.c_int), ("nT", C.c_int),
+                ("nbins", C.c_int), ("rho", C.POINTER(C.c_double)),
+                ("Tgrid", C.POINTER(C.c_double)), ("nF", C.c_int), ("F", C.c_double * 4),
+                ("group", C.c_int), ("out_group", C.POINTER(C.c_double)),
+                ("out_mean", C.POINTER(C.c_double)), ("out_sem", C.POINTER(C.c_double)),
+                ("out_leff", C.POINTER(C.c_double)), ("out_err", C.POINTER(C.c_double))]
+
+
+class ServerConfig(C.Structure):
+    """wl_server_config of wlgpu.h."""
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_double),
+                ("quantum_ms", C.c_double), ("points_per_tile", C.c_int),
+                ("ctas_per_sm", C.c_int), ("max_requests", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    """wl_server_stats of wlgpu.h."""
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong),
+                ("rejected", C.c_longlong), ("failed", C.c_longlong),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("p999_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("wall_s", C.c_double),
+                ("segments", C.c_double), ("launches", C.c_longlong),
+                ("resident_ensembles", C.c_int), ("hbm_bytes_in_use", C.c_double)]
+
+
+REQ_W, REQ_LEFF = 0, 1
+
+
 class Float4(C.Structure):
     _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float), ("w", C.c_float)]
 
@@ -125,6 +158,13 @@ def lib():
                                C.c_double, C.c_double, fp, fp]
         L.wl_last_launches.argtypes = [vp, ip, C.POINTER(C.c_char_p)]
         L.wl_legacy_configure.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int]
+        L.wl_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
+        L.wl_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_longlong)]
+        L.wl_server_wait.argtypes = [vp, C.c_longlong, C.c_double]
+        L.wl_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+        L.wl_server_last_error.argtypes = [vp, C.c_char_p, C.c_int]
+        L.wl_server_reset_stats.argtypes = [vp]
+        L.wl_server_destroy.argtypes = [vp]
         L.EV.restype = C.c_double
         L.EV.argtypes = [C.c_double, C.c_void_p, ip]
         _lib = L
@@ -343,6 +383,109 @@ class Context:
 
     def synchronize(self):
         self._check(lib().wl_ctx_synchronize(self._h))
+
+
+class Server:
+    """Continuously batched request server (wl_server): ensembles named by
+    (seed, Nl, ppl) are generated on the device at first use and stay
+    resident; requests are admitted by HBM footprint and their tiles share
+    the persistent kernel's launches with every other admitted request."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: float = 0.0,
+                 quantum_ms: float = 0.0, points_per_tile: int = 0, ctas_per_sm: int = 0,
+                 max_requests: int = 0):
+        cfg = ServerConfig(device, float(hbm_budget_bytes), float(quantum_ms),
+                           int(points_per_tile), int(ctas_per_sm), int(max_requests))
+        self._h = C.c_void_p()
+        st = lib().wl_server_create(C.byref(cfg), C.byref(self._h))
+        if st != 0:
+            raise WlError(st, "wl_server_create")
+        self._open = {}  # ticket -> (outputs, kept inputs)
+
+    def close(self):
+        if self._h:
+            lib().wl_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _error(self, st):
+        buf = C.create_string_buffer(512)
+        lib().wl_server_last_error(self._h, buf, 512)
+        return WlError(st, buf.value.decode())
+
+    def _submit(self, q, outs, keep):
+        t = C.c_longlong()
+        st = lib().wl_server_submit(self._h, C.byref(q), C.byref(t))
+        if st != 0:
+            raise self._error(st)
+        self._open[t.value] = (outs, keep)
+        return t.value
+
+    @staticmethod
+    def _base(seed, Nl, ppl, fld, F, group, kind):
+        F = _d(F)
+        q = Request()
+        q.seed, q.Nl, q.ppl, q.field, q.kind = seed, Nl, ppl, fld, kind
+        q.nF = len(F)
+        for k, f in enumerate(F[:4]):
+            q.F[k] = f
+        q.group = group
+        return q, F
+
+    def submit_w(self, seed: int, Nl: int, ppl: int, fld: Field, cx, cy, T, F,
+                 group: int = 128, want_groups: bool = False) -> int:
+        """<W> request; wait() returns (groups or None, mean, sem)."""
+        q, F = self._base(seed, Nl, ppl, fld, F, group, REQ_W)
+        cx, cy, T = _d(cx), _d(cy), _d(T)
+        n = len(T)
+        q.ninst = n
+        q.cx, q.cy, q.T = _p(cx, C.c_double), _p(cy, C.c_double), _p(T, C.c_double)
+        g = np.empty((n, len(F), max(Nl // max(group, 1), 1))) if want_groups else None
+        m, se = np.empty((n, len(F))), np.empty((n, len(F)))
+        if want_groups:
+            q.out_group = _p(g, C.c_double)
+        q.out_mean, q.out_sem = _p(m, C.c_double), _p(se, C.c_double)
+        return self._submit(q, (g, m, se), [cx, cy, T, F])
+
+    def submit_leff(self, seed: int, Nl: int, ppl: int, fld: Field, rho, T, F,
+                    group: int = 128, nbins: int = 20) -> int:
+        """Effective-action-density request; wait() returns (leff, err)."""
+        q, F = self._base(seed, Nl, ppl, fld, F, group, REQ_LEFF)
+        rho, T = _d(rho), _d(T)
+        q.nrho, q.nT, q.nbins = len(rho), len(T), nbins
+        q.rho, q.Tgrid = _p(rho, C.c_double), _p(T, C.c_double)
+        le, er = np.empty((len(rho), len(F))), np.empty((len(rho), len(F)))
+        q.out_leff, q.out_err = _p(le, C.c_double), _p(er, C.c_double)
+        return self._submit(q, (le, er), [rho, T, F])
+
+    def wait(self, ticket: int, timeout_ms: float = -1.0):
+        """The request's outputs, or None if it is not done within timeout_ms."""
+        st = lib().wl_server_wait(self._h, ticket, float(timeout_ms))
+        if st == 1:  # WL_PENDING
+            return None
+        outs, _ = self._open.pop(ticket, (None, None))
+        if st != 0:
+            raise self._error(st)
+        return outs
+
+    def reset_stats(self):
+        lib().wl_server_reset_stats(self._h)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        lib().wl_server_get_stats(self._h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
 
 
 def eval_noalloc(dev_loops: int, Nl: int, ppl: int, fld: Field, ninst: int, dev_cx: int,
