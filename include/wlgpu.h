@@ -147,7 +147,8 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
                    double *dev_out_mean, double *dev_out_sem);
 
 /* Throughput probe of one SM pipe on the context's device, for roofline
- * denominators: kind 0 = FP32 FMA, 1 = MUFU reciprocal.  *ops_per_s receives
+ * denominators: kind 0 = FP32 FMA, 1 = MUFU reciprocal, 2 = packed FP32x2 FMA
+ * (fma.rn.f32x2, two FMAs per instruction).  *ops_per_s receives
  * lane operations per second over the whole device (about 0.1 s of work). */
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s);
 

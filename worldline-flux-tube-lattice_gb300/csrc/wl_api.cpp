@@ -928,11 +928,11 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
 }
 
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s) {
-  if (!ctx || !ops_per_s || (kind != 0 && kind != 1)) return fail(ctx, WL_ERR_INVALID, "bad probe");
+  if (!ctx || !ops_per_s || kind < 0 || kind > 2) return fail(ctx, WL_ERR_INVALID, "bad probe");
   int r = set_device(ctx);
   if (r) return r;
   const int threads = 256, blocks = ctx->num_sms * 8;
-  const int iters = kind == 0 ? 4096 : 1024;
+  const int iters = kind == 1 ? 1024 : 4096;
   if (ctx->partial.reserve((size_t)blocks) != cudaSuccess) return fail(ctx, WL_ERR_NOMEM, "probe");
   float *sink = (float *)ctx->partial.p;
   cudaEvent_t e0, e1;
@@ -951,7 +951,7 @@ int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  *ops_per_s = (double)blocks * threads * iters * 8.0 / (best * 1e-3);
+  *ops_per_s = (double)blocks * threads * iters * (kind == 2 ? 16.0 : 8.0) / (best * 1e-3);
   return WL_OK;
 }
 

@@ -227,10 +227,29 @@ __global__ void peak_rcp_kernel(int iters, float *sink) {
   if (s == -1.0f) sink[blockIdx.x] = s;
 }
 
+// packed pairs: each fma.rn.f32x2 performs two FP32 FMAs (16 per iteration)
+__global__ void peak_fma2_kernel(int iters, float *sink) {
+  float2 a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    a[k] = make_float2(1.0f + 1e-7f * (float)(threadIdx.x + k), 1.0f - 1e-7f * (float)k);
+  const float2 m = make_float2(0.999999f, 0.999998f), c = make_float2(1e-7f, 2e-7f);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = __ffma2_rn(a[k], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k].x + a[k].y;
+  if (s == -1.0f) sink[blockIdx.x] = s;
+}
+
 cudaError_t launch_peak_probe(int kind, int blocks, int threads, int iters, float *sink,
                               cudaStream_t s) {
   if (kind == 0)
     peak_fma_kernel<<<blocks, threads, 0, s>>>(iters, sink);
+  else if (kind == 2)
+    peak_fma2_kernel<<<blocks, threads, 0, s>>>(iters, sink);
   else
     peak_rcp_kernel<<<blocks, threads, 0, s>>>(iters, sink);
   return cudaGetLastError();
