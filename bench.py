@@ -391,6 +391,115 @@ def run_serve(args):
                    "points_per_tile": 16384}}))
 
 
+# Algorithmic MUFU operations per segment-image of the lattice (5 nodes of the
+# Gaussian integrand, each one ex2 and one reciprocal; fixed, not tuned)
+ALG_MUFU_PER_SEG_IMAGE = 10
+
+
+def lattice_image_counts(bbox, cx, cy, T, a, lam, rimage):
+    """Images each (loop, instance) sums, as the kernel selects them: |R| <=
+    rimage and R within sqrt(18) lambda of the loop's scaled bounding box.
+    bbox: [Nl][4] unit-loop (xmin, xmax, ymin, ymax).  Returns [ninst]."""
+    f32 = np.float32
+    rr = rimage / a
+    rimg2 = f32(rr * rr * (1.0 + 1e-6))
+    lim = int(np.floor(np.sqrt(rimg2)))
+    rcut = f32(4.242640687119285 * lam)
+    inva = f32(1.0) / f32(a)
+    m = np.arange(-lim, lim + 1)
+    disk = ((m[:, None] ** 2 + m[None, :] ** 2) <= rimg2).astype(np.int64)
+    P = np.zeros((2 * lim + 2, 2 * lim + 2), np.int64)
+    P[1:, 1:] = disk.cumsum(0).cumsum(1)
+    bb = bbox.astype(f32)
+    out = np.empty(len(T), np.int64)
+    for i in range(len(T)):
+        s, x0, y0 = f32(np.sqrt(T[i])), f32(cx[i]), f32(cy[i])
+        m0 = np.maximum(-lim, np.ceil((s * bb[:, 0] + x0 - rcut) * inva)).astype(np.int64)
+        m1 = np.minimum(lim, np.floor((s * bb[:, 1] + x0 + rcut) * inva)).astype(np.int64)
+        n0 = np.maximum(-lim, np.ceil((s * bb[:, 2] + y0 - rcut) * inva)).astype(np.int64)
+        n1 = np.minimum(lim, np.floor((s * bb[:, 3] + y0 + rcut) * inva)).astype(np.int64)
+        ok = (m0 <= m1) & (n0 <= n1)
+        m0, m1, n0, n1 = m0 + lim, m1 + lim + 1, n0 + lim, n1 + lim + 1
+        c = P[m1, n1] - P[m0, n1] - P[m1, n0] + P[m0, n0]
+        out[i] = int(np.where(ok, c, 0).sum())
+    return out
+
+
+def run_lattice(args):
+    """Square lattice of Gaussian tubes (lambda = 1, F = 1, images to 12a):
+    Nl = 8192 x ppl = 4096 (seed 3), 96 log-spaced T in [1e-2, 1e2], a 4 x 4
+    grid of centres over one unit cell (the configuration's 32 x 32 grid
+    subsampled to keep the run within minutes), a in {2, 5, 10}, scalar and
+    spinor; one timed evaluation per case after a warm-up."""
+    import torch
+
+    import wltube
+
+    Nl, ppl, seed, nT, ngrid = 8192, 4096, 3, 96, args.lattice_grid
+    ctx = wltube.Context(0)
+    h = ctx.generate(seed, Nl, ppl)
+    host = ctx.download(h)
+    bbox = np.stack([host[:, :, 0].min(1), host[:, :, 0].max(1),
+                     host[:, :, 1].min(1), host[:, :, 1].max(1)], axis=1)
+    del host
+    Tg = np.geomspace(1e-2, 1e2, nT)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    mufu_peak = ctx.peak_probe(1)
+    cases = []
+    for a in (2.0, 5.0, 10.0):
+        u = (np.arange(ngrid) + 0.5) / ngrid * a
+        gx, gy = np.meshgrid(u, u, indexing="ij")
+        cx = np.repeat(gx.ravel(), nT)
+        cy = np.repeat(gy.ravel(), nT)
+        T = np.tile(Tg, ngrid * ngrid)
+        n = len(T)
+        imgs = lattice_image_counts(bbox, cx, cy, T, a, 1.0, 12.0 * a)
+        dcx = torch.tensor(cx, dtype=torch.float64, device="cuda")
+        dcy = torch.tensor(cy, dtype=torch.float64, device="cuda")
+        dT = torch.tensor(T, dtype=torch.float64, device="cuda")
+        dm = torch.empty(n, dtype=torch.float64, device="cuda")
+        ds = torch.empty(n, dtype=torch.float64, device="cuda")
+        for fe in (0, 1):
+            fld = wltube.field("lattice", fermion=fe, nint=NINT, lambda2=1.0, tubedist=a)
+            # warm-up on the smallest proper times (few images)
+            ctx.eval_device(h, fld, 16, dcx.data_ptr(), dcy.data_ptr(), dT.data_ptr(), [1.0],
+                            GROUP, 0, dm.data_ptr(), ds.data_ptr())
+            ctx.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            clocks = Clocks(0)
+            e0.record(stream)
+            ctx.eval_device(h, fld, n, dcx.data_ptr(), dcy.data_ptr(), dT.data_ptr(), [1.0],
+                            GROUP, 0, dm.data_ptr(), ds.data_ptr())
+            e1.record(stream)
+            ctx.synchronize()
+            torch.cuda.synchronize()
+            clk = clocks.stop()
+            ms = e0.elapsed_time(e1)
+            segs = n * Nl * ppl
+            seg_img = int(imgs.sum()) * ppl
+            cases.append({"a": a, "fermion": fe, "instances": n, "ms": ms,
+                          "segments_per_s": segs / (ms * 1e-3),
+                          "segment_images_per_s": seg_img / (ms * 1e-3),
+                          "mean_images_per_segment": seg_img / segs,
+                          "mufu_frac": seg_img / (ms * 1e-3) * ALG_MUFU_PER_SEG_IMAGE / mufu_peak,
+                          "W_mean_sample": float(dm[n // 2].item()), "clocks": clk})
+            sys.stderr.write("lattice a=%g fermion=%d: %.0f ms\n" % (a, fe, ms))
+    print(json.dumps({
+        "metric": "lattice: loop-segments/s and segment-image evaluations/s",
+        "value": float(np.sum([c["instances"] * Nl * ppl for c in cases]) /
+                       (np.sum([c["ms"] for c in cases]) * 1e-3)),
+        "unit": "segments/s", "cases": cases,
+        "roofline": {"bound": "mufu", "alg_mufu_per_segment_image": ALG_MUFU_PER_SEG_IMAGE,
+                     "peak_mufu_ops_per_s": mufu_peak,
+                     "peak_source": "MUFU rcp probe measured in this run"},
+        "config": {"workload": "square lattice of Gaussian tubes, lambda=1, F=1, images to "
+                               "|R|<=12a, Nl=8192 x ppl=4096 (seed 3), 96 log T in [1e-2,1e2], "
+                               "%dx%d centres over one unit cell, a in {2,5,10}, scalar and "
+                               "spinor, 5 Simpson nodes, exact mode" % (ngrid, ngrid)}}))
+    ctx.release(h)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,11 +511,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 128 instances on the full ensemble, no e2e/cpu")
-    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "serve"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "serve", "lattice"],
                     help="c2: the headline spinor workload; batch: uneven multi-job batch; "
                          "serve: Poisson request stream through the server")
     ap.add_argument("--jobs", type=int, default=32, help="jobs of the batch workload")
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
+    ap.add_argument("--lattice-grid", type=int, default=4,
+                    help="centres per side of the unit cell (lattice workload)")
     ap.add_argument("--serve-profiles", default="smooth,gaussian",
                     help="profiles of the served requests (lattice requests cost up to "
                          "hundreds of single-tube segments each: one per image)")
@@ -418,6 +529,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "lattice":
+        run_lattice(args)
         return
     world, rank, local = dist_setup()
     if args.impl == "reference":

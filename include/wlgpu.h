@@ -50,9 +50,10 @@ extern "C" {
  * reference's single-tube Gaussian segment integral (intEV.cu:408-459,
  * 282-284) in coordinates relative to R.  Exact mode only: the reference's
  * b >= 1e-8 clamp would break the pure-gauge cancellation of distant images.
- * Images farther than sqrt(30) lambda from the loop's bounding box see
- * f = 1 - e^-30 along the whole loop and lie outside it (winding 0): their
- * exact contribution is zero and they are skipped. */
+ * Images farther than sqrt(18) lambda from the loop's bounding box see
+ * f = 1 - e^-18 along the whole loop, which is 1 in FP32 (pure gauge), and
+ * lie outside it (winding 0): their continuum contribution is zero and they
+ * are skipped. */
 #define WL_PROFILE_LATTICE 8
 
 /* clamp modes of the segment polynomial */

@@ -96,6 +96,7 @@ def lib():
         L.wlo64_fl_over_rho2.restype = C.c_double
         L.wlo64_fl_over_rho2.argtypes = [C.c_double, Fp]
         L.wlo64_idt.argtypes = [C.c_double, C.c_double, C.c_double, Fp, dp, dp]
+        L.wlo_set_lattice_rcut.argtypes = [C.c_double]
         L.wlo64_loop_sums.argtypes = [fp, C.c_int, C.c_double, C.c_double, C.c_double,
                                       Fp, dp, dp]
         L.wlo32_loop_sums.argtypes = [fp, C.c_int, C.c_float, C.c_float, C.c_float,
@@ -145,6 +146,15 @@ def _ptr(a, t):
 
 
 QED = Qed(QED_M2, QED_E)
+
+
+LATTICE_RCUT_L = 4.242640687119285  # sqrt(18): images beyond are pure gauge in FP32
+
+
+def set_lattice_rcut(r_over_lambda: float):
+    """Near-image margin of the lattice sum in units of lambda (<= 0: every
+    image with |R| <= rimage)."""
+    lib().wlo_set_lattice_rcut(C.c_double(r_over_lambda))
 
 
 def philox(ctr, key):

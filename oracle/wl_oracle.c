@@ -75,12 +75,16 @@ void wlo64_idt(double a, double b, double c, const wlo_field *f, double *scalI,
 }
 
 /* square lattice of Gaussian tubes (see wl_oracle.h) */
+static double g_lattice_rcut = WLO_LATTICE_RCUT_L;
+
+void wlo_set_lattice_rcut(double r_over_lambda) { g_lattice_rcut = r_over_lambda; }
+
 static void d_lattice_sums(const float *w, int ppl, double cx, double cy, double rtT,
                            const wlo_field *f, double gs[3], double gf[3]) {
   wlo_field g = *f;
   g.profile = WLO_GAUSSIAN;
   g.mode = WLO_EXACT;
-  const double a = f->tubedist, rcut = WLO_LATTICE_RCUT_L * sqrt(f->lambda2);
+  const double a = f->tubedist, rcut = g_lattice_rcut * sqrt(f->lambda2);
   double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
   for (int i = 0; i < ppl; i++) {
     double x = cx + rtT * (double)w[4 * i], y = cy + rtT * (double)w[4 * i + 1];
@@ -89,9 +93,10 @@ static void d_lattice_sums(const float *w, int ppl, double cx, double cy, double
     ymin = fmin(ymin, y);
     ymax = fmax(ymax, y);
   }
-  const int m0 = (int)ceil((xmin - rcut) / a), m1 = (int)floor((xmax + rcut) / a);
-  const int n0 = (int)ceil((ymin - rcut) / a), n1 = (int)floor((ymax + rcut) / a);
   const double rr = f->rimage / a;
+  int m0 = (int)ceil((xmin - rcut) / a), m1 = (int)floor((xmax + rcut) / a);
+  int n0 = (int)ceil((ymin - rcut) / a), n1 = (int)floor((ymax + rcut) / a);
+  if (g_lattice_rcut <= 0.0) m0 = n0 = -(int)floor(rr), m1 = n1 = (int)floor(rr);
   gs[0] = gs[1] = gs[2] = 0;
   gf[0] = gf[1] = gf[2] = 0;
   for (int m = m0; m <= m1; m++)

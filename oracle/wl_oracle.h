@@ -57,10 +57,14 @@ typedef struct {
  * f = 1 - exp(-rho^2/lambda^2), intEV.cu:282-284) in coordinates relative to
  * R, in exact mode (no clamps: the reference's b >= 1e-8 clamp would break
  * the pure-gauge cancellation of distant images).  Images farther than
- * WLO_LATTICE_RCUT_L * lambda from the loop's bounding box see f = 1 (to
- * e^-30) along the whole loop and lie outside it (winding 0): their exact
- * contribution is zero and they are skipped.                                */
-#define WLO_LATTICE_RCUT_L 5.477225575051661 /* sqrt(30) */
+ * rcut = sqrt(18) lambda from the loop's bounding box see x = rho^2/lambda^2
+ * >= 18 along the whole loop, where f = 1 - e^-x rounds to 1 in FP32 (e^-18 <
+ * 2^-25): pure gauge, and the loop does not wind around them, so their
+ * continuum contribution is zero and they are skipped.
+ * wlo_set_lattice_rcut(r) sets rcut / lambda (r <= 0: sum every image with
+ * |R| <= rimage), which the tests use to check the selection.              */
+#define WLO_LATTICE_RCUT_L 4.242640687119285 /* sqrt(18) */
+void wlo_set_lattice_rcut(double r_over_lambda);
 
 /* ---- profiles (FP64) -------------------------------------------------- */
 double wlo64_flambda(double rho2, const wlo_field *f);

@@ -92,3 +92,70 @@ def test_library_matches_reference_kernel_per_loop(refgpu):
             ran += 1
         ctx.release(h)
     assert ran >= 8
+
+
+def test_reference_kernel_throughput_vs_library(refgpu, capsys):
+    """The reference's own kernel (smooth, spinor, its 50 Simpson intervals,
+    512 threads per block as EffAct.c sets them, one launch per instance as
+    EV() makes them) against the library's sweep at the same 50 intervals, on
+    the spinor benchmark ensemble (Nl 5120 x ppl 2048, seed 2).  Both are
+    timed with CUDA events around their launches only."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    import wltube
+
+    cub = os.path.join(O.REF_DIR, "ref_smooth.cubin")
+    if not os.path.exists(cub):
+        pytest.skip("reference smooth cubin not built")
+    Nl, ppl, F = 5120, 2048, 1.0
+    with wltube.Context(0) as ctx:
+        h = ctx.generate(2, Nl, ppl)
+        wl = torch.from_numpy(ctx.download(h)).cuda()          # 5120 = 10 blocks of 512
+        scal = torch.zeros((Nl, 4), dtype=torch.float32, device="cuda")
+        ferm = torch.zeros((Nl, 4), dtype=torch.float32, device="cuda")
+        kh = refgpu.refgpu_load(cub.encode(), 0)
+        assert kh >= 0
+        sample = [(r, t) for r in (0.0, 2.0, 4.0, 8.0) for t in (0.01, 1.0)]
+        ms = C.c_float()
+        r, t = sample[0]                                         # warm-up launch
+        assert refgpu.refgpu_run(kh, scal.data_ptr(), ferm.data_ptr(), wl.data_ptr(), r, 0.0, F,
+                                 1.0, float(np.float32(np.sqrt(t))), Nl, ppl, 1, 512, Nl,
+                                 C.byref(ms)) == 0
+        ref_ms = 0.0
+        for r, t in sample:
+            rc = refgpu.refgpu_run(kh, scal.data_ptr(), ferm.data_ptr(), wl.data_ptr(), r, 0.0,
+                                   F, 1.0, float(np.float32(np.sqrt(t))), Nl, ppl, 1, 512, Nl,
+                                   C.byref(ms))
+            assert rc == 0, rc
+            ref_ms += ms.value
+        ref_rate = len(sample) * Nl * ppl / (ref_ms * 1e-3)
+
+        n = 512
+        rho = np.repeat(np.linspace(0.0, 8.0, 16), n // 16)
+        T = np.tile(np.geomspace(1e-3, 1e3, n // 16), 16)
+        fld = wltube.field("smooth", fermion=1, nint=50)
+        dcx = torch.tensor(rho, dtype=torch.float64, device="cuda")
+        dcy = torch.zeros(n, dtype=torch.float64, device="cuda")
+        dT = torch.tensor(T, dtype=torch.float64, device="cuda")
+        dm = torch.empty(n, dtype=torch.float64, device="cuda")
+        ds = torch.empty(n, dtype=torch.float64, device="cuda")
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        args = (h, fld, n, dcx.data_ptr(), dcy.data_ptr(), dT.data_ptr(), [F], 128, 0,
+                dm.data_ptr(), ds.data_ptr())
+        ctx.eval_device(*args)
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.eval_device(*args)
+        e1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        lib_rate = n * Nl * ppl / (e0.elapsed_time(e1) * 1e-3)
+        ctx.release(h)
+    with capsys.disabled():
+        print(json.dumps({"reference_kernel_segments_per_s": ref_rate,
+                          "library_segments_per_s": lib_rate, "speedup": lib_rate / ref_rate,
+                          "simpson_intervals": 50, "reference_sample_instances": len(sample),
+                          "library_instances": n}))
+    assert lib_rate > 10 * ref_rate

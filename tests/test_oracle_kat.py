@@ -91,3 +91,24 @@ def test_tfunc_regimes_follow_reference_thresholds():
     assert O.tfunc_regime(60.0, 0.0, 0.0, 1.0, fld)[0] == 2    # large T
     fld2 = O.field("smooth", fermion=0, lambda2=100.0)
     assert O.tfunc_regime(0.2, 0.0, 0.0, 1.0, fld2)[0] == 1    # const field (T >= 0.1)
+
+
+def test_lattice_image_selection_matches_full_sum():
+    """Skipping the images farther than sqrt(18) lambda from the loop's
+    bounding box (pure gauge in FP32, winding 0) leaves the per-loop phases
+    and spin exponents of the full image sum (|R| <= 12 a) unchanged to the
+    Simpson discretisation error of those pure-gauge images, which 50
+    intervals make negligible."""
+    L = O.vloops(3, 24, 128)
+    try:
+        for a, T in ((2.0, 0.05), (2.0, 3.0), (5.0, 10.0)):
+            fld = O.field("lattice", fermion=1, nint=50, mode=1, lambda2=1.0, tubedist=a)
+            O.set_lattice_rcut(O.LATTICE_RCUT_L)
+            s_cut, f_cut = O.loops_phases(L, 0.3 * a, 0.6 * a, T, 1.0, fld)
+            O.set_lattice_rcut(0.0)
+            s_all, f_all = O.loops_phases(L, 0.3 * a, 0.6 * a, T, 1.0, fld)
+            scale = np.abs(s_all).max()
+            assert np.abs(s_cut - s_all).max() < 1e-6 * max(scale, 1.0), (a, T)
+            assert np.abs(f_cut - f_all).max() < 1e-6 * max(np.abs(f_all).max(), 1.0), (a, T)
+    finally:
+        O.set_lattice_rcut(O.LATTICE_RCUT_L)

@@ -67,12 +67,14 @@ struct wl_ctx {
   DevBuf<double> out;       // group values, means, SEMs
   DevBuf<int> status;       // device status word
   DevBuf<int> list;         // EV() loop list
+  DevBuf<int> perm;         // lattice: instances in decreasing proper time
   DevBuf<double> aux;       // proper-time integral inputs and outputs
   // batches: instances, partial sums, outputs, descriptors (jobs, tiles,
   // reduce jobs, queue counter)
   DevBuf<float> b_inst;
   DevBuf<double> b_part, b_out;
   DevBuf<unsigned char> b_meta;
+  DevBuf<int> b_perm;
   int tune_points = 16384;  // points per tile target (autotuned)
   int tune_ctas = 0;        // persistent CTAs per SM, 0 = occupancy limit
   double last_batch_ms = 0.0;
@@ -175,7 +177,7 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
   if (p == WL_PROFILE_LATTICE) {
     const double rr = f->rimage / f->tubedist;
     d->rimg2 = (float)(rr * rr * (1.0 + 1e-6));
-    d->rcut = (float)(5.477225575051661 * sqrt(f->lambda2));  // sqrt(30) lambda
+    d->rcut = (float)(4.242640687119285 * sqrt(f->lambda2));  // sqrt(18) lambda
   }
   if (f->mode == WL_MODE_REFCOMPAT) {
     d->clampA = d->clampB = d->clampC = d->clampE = 1.0e-8f;
@@ -343,6 +345,7 @@ int batch_loops_per_tile(int points_per_tile, int ppl, int group) {
 }
 
 struct BatchPlan {
+  size_t perm_total = 0;  // lattice jobs' instance orders
   std::vector<wl::SweepArgs> jobs;
   std::vector<wl::BatchTile> tiles;
   std::vector<wl::ReduceJob> rjobs;
@@ -417,6 +420,9 @@ int batch_plan(wl_ctx *ctx, int njobs, const wl_job *jobs, int points, BatchPlan
     if (kprofs[i] == wl::kLattice) {
       int rb = ensure_bbox(ctx, J.handle, &a.bbox);
       if (rb) return rb;
+      // offset + 1 now (0 = none); patched into a device pointer later
+      a.perm = (const int *)(uintptr_t)(P->perm_total + 1);
+      P->perm_total += (size_t)n;
     }
     wl::ReduceJob &rj = P->rjobs[i];
     rj.n_chunks = a.n_chunks;
@@ -455,7 +461,8 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
   if (ctx->b_inst.reserve(P.inst.size()) != cudaSuccess ||
       ctx->b_part.reserve(P.part_total) != cudaSuccess ||
       ctx->b_out.reserve(P.out_total) != cudaSuccess ||
-      ctx->b_meta.reserve(meta_bytes) != cudaSuccess) {
+      ctx->b_meta.reserve(meta_bytes) != cudaSuccess ||
+      (P.perm_total && ctx->b_perm.reserve(P.perm_total) != cudaSuccess)) {
     cudaGetLastError();
     return fail(ctx, WL_ERR_NOMEM, "cannot allocate the batch buffers");
   }
@@ -471,6 +478,7 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
     a.tql = a.cx + 4 * n;
     a.partial = ctx->b_part.p + (size_t)(uintptr_t)a.partial;
     a.status = ctx->status.p;
+    if (a.perm) a.perm = ctx->b_perm.p + ((size_t)(uintptr_t)a.perm - 1);
     wl::ReduceJob &rj = P.rjobs[i];
     rj.partial = a.partial;
     const int ng = a.Nl / rj.lpg;
@@ -487,6 +495,10 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
   WL_CHECK(ctx, cudaMemcpyAsync(meta + off_rj, P.rjobs.data(), rj_bytes, cudaMemcpyHostToDevice,
                                 ctx->stream));
   WL_CHECK(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+  for (int i = 0; i < njobs; ++i)  // lattice jobs: instances in decreasing proper time
+    if (P.jobs[i].perm)
+      WL_CHECK(ctx, wl::launch_order_by_T(P.jobs[i].rtT, P.jobs[i].ninst,
+                                          const_cast<int *>(P.jobs[i].perm), ctx->stream));
   WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));  // host vectors are released on return
 
   wl::BatchArgs B;
@@ -626,6 +638,8 @@ int wl_ctx_destroy(wl_ctx *ctx) {
   ctx->out.release();
   ctx->status.release();
   ctx->list.release();
+  ctx->perm.release();
+  ctx->b_perm.release();
   ctx->aux.release();
   ctx->b_inst.release();
   ctx->b_part.release();
@@ -829,6 +843,14 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
     a.status = ctx->status.p;
     a.wait_tries = 1u << 22;
     a.bbox = bbox;
+    if (kprof == wl::kLattice) {  // warps of similar image counts
+      if (ctx->perm.reserve((size_t)ninst) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, WL_ERR_NOMEM, "cannot allocate the instance order");
+      }
+      WL_CHECK(ctx, wl::launch_order_by_T(a.rtT, ninst, ctx->perm.p, ctx->stream));
+      a.perm = ctx->perm.p;
+    }
     WL_CHECK(ctx, wl::launch_sweep(kprof, fermion, nint, a, ctx->stream));
     ctx->last_kind = "instance-parallel";
   } else {

@@ -316,12 +316,17 @@ __device__ __forceinline__ ImgRange image_range(float4 bb, float s, float cx, fl
   return r;
 }
 
-// (1 - e^-x)/x and e^-x for x >= 0 (x slightly below 0 from rounding is fine)
+// (1 - e^-x)/x and e^-x for x >= 0 (x slightly below 0 from rounding is fine).
+// Below x = 0.5 (a node within 0.7 lambda of a tube's centre) the series
+// replaces 1 - e^-x, whose cancellation would cost up to 2^-22/x relative;
+// the series is evaluated only when some active lane of the warp needs it
+// (most image segments stay far from every core).
 __device__ __forceinline__ void gauss_q(float x, float &q, float &e) {
   e = expneg_fast(x);
-  const float big = (1.0f - e) * rcp_fast(x);
-  const float small = one_minus_expneg_over_x(x);
-  q = x < 0.5f ? small : big;
+  q = (1.0f - e) * rcp_fast(x);
+  if (__any_sync(__activemask(), x < 0.5f)) {
+    if (x < 0.5f) q = one_minus_expneg_over_x(x);
+  }
 }
 
 // One segment z_i -> z_j against every image of the range: in units of

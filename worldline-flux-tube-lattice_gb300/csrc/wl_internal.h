@@ -44,6 +44,9 @@ struct SweepArgs {
   uint32_t wait_tries;
   int kprof, fermion, nint;  // kernel selection inside the persistent batch kernel
   const float4 *bbox;        // lattice: [Nl] unit-loop (xmin, xmax, ymin, ymax)
+  // optional [ninst] thread slot -> instance: lattice instances ordered by
+  // proper time so that the threads of a warp sum similar numbers of images
+  const int *perm;
 };
 
 // Persistent multi-job sweep: a queue of tiles (job, instance tile, loop
@@ -137,6 +140,10 @@ struct TintArgs {
   double *leff, *err;  // [nrho][nF]
 };
 cudaError_t launch_tint(const TintArgs &a, cudaStream_t s);
+
+// perm[0..n) = instances in decreasing rtT (one CTA, bucketed by log2 rtT;
+// the order inside a bucket is arbitrary and changes no result)
+cudaError_t launch_order_by_T(const float *rtT, int n, int *perm, cudaStream_t s);
 
 // per-loop bounding boxes of an ensemble (lattice image selection)
 cudaError_t launch_loop_bbox(const float4 *loops, int Nl, int ppl, float4 *out, cudaStream_t s);

@@ -87,6 +87,40 @@ __global__ void group_reduce_kernel(const double *__restrict__ partial, int n_ch
     out_sem[(size_t)inst * nF + j] = ng > 1 ? sqrt(ss / ((double)ng * (ng - 1.0))) : 0.0;
 }
 
+// ------------------------------------------------ lattice instance order --
+constexpr int kOrderBuckets = 512;  // log2(rtT) in steps of 1/16 over [-16, 16)
+
+__device__ __forceinline__ int order_bucket(float rtT) {
+  const float x = log2f(fmaxf(rtT, 1e-30f)) * 16.0f;
+  const int b = min(max((int)floorf(x) + kOrderBuckets / 2, 0), kOrderBuckets - 1);
+  return kOrderBuckets - 1 - b;  // largest proper times first
+}
+
+__global__ void __launch_bounds__(1024) order_by_T_kernel(const float *__restrict__ rtT, int n,
+                                                          int *__restrict__ perm) {
+  __shared__ int cnt[kOrderBuckets];
+  for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) cnt[b] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&cnt[order_bucket(rtT[i])], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int b = 0; b < kOrderBuckets; ++b) {
+      const int c = cnt[b];
+      cnt[b] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    perm[atomicAdd(&cnt[order_bucket(rtT[i])], 1)] = i;
+}
+
+cudaError_t launch_order_by_T(const float *rtT, int n, int *perm, cudaStream_t s) {
+  order_by_T_kernel<<<1, 1024, 0, s>>>(rtT, n, perm);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_group_reduce(const double *partial, int n_chunks, int cpg, int lpg,
                                 int ninst, int nF, double *out_group, double *out_mean,
                                 double *out_sem, cudaStream_t s) {

@@ -82,7 +82,7 @@ struct Req {
   int ninst = 0, lc = 0, n_chunks = 0, ng = 0, tiles_x = 0;
   long long ntiles = 0, next_tile = 0;
   size_t dbytes = 0, pbytes = 0;  // device / pinned footprint
-  size_t o_rj = 0, o_inst = 0, o_part = 0, o_out = 0, o_aux = 0;  // device offsets
+  size_t o_rj = 0, o_inst = 0, o_perm = 0, o_part = 0, o_out = 0, o_aux = 0;  // device offsets
   size_t p_args = 0, p_rj = 0, p_inst = 0, p_aux = 0, n_aux_in = 0, p_out = 0, n_out = 0;
   double tile_work = 0.0, segments = 0.0;
   // admitted state
@@ -234,7 +234,9 @@ int check_request(wl_server *s, const wl_request *q, Req *R) {
   }
   R->o_rj = up(sizeof(int));
   R->o_inst = R->o_rj + up(sizeof(wl::ReduceJob));
-  R->o_part = R->o_inst + up(sizeof(float) * wl::kInstArrays * n);
+  R->o_perm = R->o_inst + up(sizeof(float) * wl::kInstArrays * n);
+  const size_t n_perm = R->kprof == wl::kLattice ? (size_t)n : 0;
+  R->o_part = R->o_perm + up(sizeof(int) * n_perm);
   R->o_out = R->o_part + up(sizeof(double) * n_part);
   R->o_aux = R->o_out + up(sizeof(double) * n_out);
   R->dbytes = R->o_aux + up(sizeof(double) * n_aux);
@@ -437,6 +439,7 @@ bool admit(wl_server *s) {
     a.fermion = R->q.field.fermion != 0;
     a.nint = R->q.field.nint;
     a.bbox = E->bbox;
+    if (R->kprof == wl::kLattice) a.perm = (const int *)(dmem + R->o_perm);
     wl::ReduceJob &rj = R->rj;
     memset(&rj, 0, sizeof(rj));
     rj.partial = d_part;
@@ -486,8 +489,10 @@ bool admit(wl_server *s) {
     }
     ck(cudaMemcpyAsync(s->d_slots + R->slot, pin + R->p_args, sizeof(wl::SweepArgs),
                        cudaMemcpyHostToDevice, s->cs), "slot upload");
-    ck(cudaMemcpyAsync(dmem + R->o_rj, pin + R->p_rj, R->o_part - R->o_rj,
+    ck(cudaMemcpyAsync(dmem + R->o_rj, pin + R->p_rj, R->o_perm - R->o_rj,
                        cudaMemcpyHostToDevice, s->cs), "request upload");
+    if (a.perm)  // lattice: instances in decreasing proper time
+      ck(wl::launch_order_by_T(a.rtT, n, const_cast<int *>(a.perm), s->cs), "instance order");
     if (R->n_aux_in)
       ck(cudaMemcpyAsync(dmem + R->o_aux, pin + R->p_aux, sizeof(double) * R->n_aux_in,
                          cudaMemcpyHostToDevice, s->cs), "grid upload");

@@ -50,8 +50,12 @@ template <int P, bool FERM, int NINT>
 __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int chunk,
                                            const SweepShared &S, int &consumed) {
   const int tid = threadIdx.x;
-  const int inst = tile_x * kSweepThreads + tid;
-  const int ic = inst < A.ninst ? inst : A.ninst - 1;
+  const int slot = tile_x * kSweepThreads + tid;
+  const bool live = slot < A.ninst;
+  const int sl = live ? slot : A.ninst - 1;
+  // every per-instance read and the partial-sum write go through ic: a
+  // thread's result does not depend on which slot it runs in
+  const int ic = A.perm ? A.perm[sl] : sl;
   const int l0 = chunk * A.chunk_loops;
   const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
   const int K = A.chunk_loops * nck;
@@ -197,9 +201,9 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
   }
   consumed = base + K;
 
-  if (inst < A.ninst) {
+  if (live) {
     for (int r = 0; r < A.nF * 3; ++r)
-      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + inst] = S.sacc[r][tid];
+      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + ic] = S.sacc[r][tid];
   }
   return true;
 }

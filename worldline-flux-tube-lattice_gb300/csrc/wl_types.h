@@ -29,7 +29,8 @@ struct FieldDev {
   int nint;  // Simpson intervals (used by the run-time-n kernels)
   float h;   // 1.0f / nint
   // lattice: images with m^2 + n^2 <= rimg2 (|R| <= rimage), near-image
-  // margin rcut = sqrt(30) lambda around the loop's bounding box
+  // margin rcut = sqrt(18) lambda around the loop's bounding box (beyond it
+  // 1 - e^{-rho^2/lambda^2} rounds to 1 in FP32: the image is pure gauge)
   float rimg2, rcut;
 };
 
