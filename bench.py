@@ -58,9 +58,10 @@ ALG_BYTES_PER_POINT = 16
 
 
 def workload(small=False):
-    """(cx, cy, T) of every instance; small: 8 T x 16 rho of the same ranges
-    (the profiling case: one instance tile, same ensemble)."""
-    nt, nrho = (8, 16) if small else (NT, NRHO)
+    """(cx, cy, T) of every instance; small: 32 T x 16 rho of the same ranges
+    (the profiling case: four instance tiles, about 2.8 waves of CTAs, same
+    ensemble)."""
+    nt, nrho = (32, 16) if small else (NT, NRHO)
     T = np.geomspace(1e-3, 1e3, nt)
     rho = np.linspace(0.0, 8.0, nrho)
     cx = np.repeat(rho, nt)
@@ -446,7 +447,8 @@ def run_lattice(args):
     stream = torch.cuda.ExternalStream(ctx.stream())
     mufu_peak = ctx.peak_probe(1)
     cases = []
-    for a in (2.0, 5.0, 10.0):
+    wanted = [(float(c.split(":")[0]), int(c.split(":")[1])) for c in args.lattice_cases.split(",")]
+    for a in sorted({a for a, _ in wanted}):
         u = (np.arange(ngrid) + 0.5) / ngrid * a
         gx, gy = np.meshgrid(u, u, indexing="ij")
         cx = np.repeat(gx.ravel(), nT)
@@ -459,7 +461,7 @@ def run_lattice(args):
         dT = torch.tensor(T, dtype=torch.float64, device="cuda")
         dm = torch.empty(n, dtype=torch.float64, device="cuda")
         ds = torch.empty(n, dtype=torch.float64, device="cuda")
-        for fe in (0, 1):
+        for fe in sorted({f for aa, f in wanted if aa == a}):
             fld = wltube.field("lattice", fermion=fe, nint=NINT, lambda2=1.0, tubedist=a)
             # warm-up on the smallest proper times (few images)
             ctx.eval_device(h, fld, 16, dcx.data_ptr(), dcy.data_ptr(), dT.data_ptr(), [1.0],
@@ -494,8 +496,8 @@ def run_lattice(args):
                      "peak_source": "MUFU rcp probe measured in this run"},
         "config": {"workload": "square lattice of Gaussian tubes, lambda=1, F=1, images to "
                                "|R|<=12a, Nl=8192 x ppl=4096 (seed 3), 96 log T in [1e-2,1e2], "
-                               "%dx%d centres over one unit cell, a in {2,5,10}, scalar and "
-                               "spinor, 5 Simpson nodes, exact mode" % (ngrid, ngrid)}}))
+                               "%dx%d centres over one unit cell, (a, fermion) in %s, 5 Simpson "
+                               "nodes, exact mode" % (ngrid, ngrid, args.lattice_cases)}}))
     ctx.release(h)
     ctx.close()
 
@@ -518,6 +520,8 @@ def main():
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
     ap.add_argument("--lattice-grid", type=int, default=4,
                     help="centres per side of the unit cell (lattice workload)")
+    ap.add_argument("--lattice-cases", default="2:0,2:1,5:0,5:1,10:0,10:1",
+                    help="a:fermion pairs of the lattice workload")
     ap.add_argument("--serve-profiles", default="smooth,gaussian",
                     help="profiles of the served requests (lattice requests cost up to "
                          "hundreds of single-tube segments each: one per image)")

@@ -152,8 +152,12 @@ struct Profile<kGaussian> {  // f = 1 - e^{-r2/l2} (intEV.cu:282-284, 383-385)
                                               float &fp) {
     const float x = r2 * F.inv_l2;
     const float e = expneg_fast(x);
-    // below x = 0.5 the series avoids the cancellation of 1 - e^-x
-    g = (x < 0.5f) ? one_minus_expneg_over_x(x) * F.inv_l2 : (1.0f - e) * rcp_fast(r2);
+    g = (1.0f - e) * rcp_fast(r2);
+    // below x = 0.5 the series avoids the cancellation of 1 - e^-x; it is
+    // evaluated only when some active lane of the warp needs it
+    if (__any_sync(__activemask(), x < 0.5f)) {
+      if (x < 0.5f) g = one_minus_expneg_over_x(x) * F.inv_l2;
+    }
     fp = e;
   }
   static __device__ __forceinline__ float fp_scale(const FieldDev &F) { return F.inv_l2; }
@@ -317,15 +321,23 @@ __device__ __forceinline__ ImgRange image_range(float4 bb, float s, float cx, fl
 }
 
 // (1 - e^-x)/x and e^-x for x >= 0 (x slightly below 0 from rounding is fine).
-// Below x = 0.5 (a node within 0.7 lambda of a tube's centre) the series
-// replaces 1 - e^-x, whose cancellation would cost up to 2^-22/x relative;
-// the series is evaluated only when some active lane of the warp needs it
-// (most image segments stay far from every core).
+// From x = 18 on, 1 - e^-x rounds to 1 in FP32 (e^-18 < 2^-25): the node is
+// pure gauge, q = 1/x, and e (below 1.6e-8) is taken as 0, so e^-x is only
+// evaluated when some active lane of the warp has x < 18.  Below x = 0.5 (a
+// node within 0.7 lambda of a tube's centre) the series replaces 1 - e^-x,
+// whose cancellation would cost up to 2^-22/x relative; it too is evaluated
+// only when some lane needs it.  Each lane's values depend on its own x only.
 __device__ __forceinline__ void gauss_q(float x, float &q, float &e) {
-  e = expneg_fast(x);
-  q = (1.0f - e) * rcp_fast(x);
-  if (__any_sync(__activemask(), x < 0.5f)) {
-    if (x < 0.5f) q = one_minus_expneg_over_x(x);
+  q = rcp_fast(x);
+  e = 0.0f;
+  if (__any_sync(__activemask(), x < 18.0f)) {
+    if (x < 18.0f) {
+      e = expneg_fast(x);
+      q *= 1.0f - e;
+    }
+    if (__any_sync(__activemask(), x < 0.5f)) {
+      if (x < 0.5f) q = one_minus_expneg_over_x(x);
+    }
   }
 }
 
