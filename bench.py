@@ -231,8 +231,10 @@ def c4_jobs(wltube, ctx, njobs, seed=4, profiles=("smooth", "gaussian")):
             ens[key] = ctx.generate(seed, Nl, ppl)
         T = np.geomspace(1e-2, 1e2, nT)
         rho = np.linspace(0.0, 5.0 * lam, nrho)
+        kw = {"tubedist": 5.0 * lam} if prof == "lattice" else {}
         jobs.append({"handle": ens[key], "field": wltube.field(prof, fermion=1, nint=NINT,
-                                                               lambda2=lam * lam),
+                                                               lambda2=lam * lam, **kw),
+                     "profile": prof,
                      "cx": np.repeat(rho, nT), "cy": np.zeros(nrho * nT),
                      "T": np.tile(T, nrho), "F": [F], "group": 128,
                      "segments": Nl * ppl * nT * nrho})
@@ -245,7 +247,8 @@ def run_batch(args):
     import wltube
 
     ctx = wltube.Context(0)
-    jobs, ens = c4_jobs(wltube, ctx, args.jobs)
+    profiles = tuple(args.batch_profiles.split(","))
+    jobs, ens = c4_jobs(wltube, ctx, args.jobs, profiles=profiles)
     total = sum(j["segments"] for j in jobs)
     # autotune on a sample: the first jobs with every 8th instance
     sample = [dict(j, cx=j["cx"][::8], cy=j["cy"][::8], T=j["T"][::8]) for j in jobs[:8]]
@@ -259,14 +262,16 @@ def run_batch(args):
     st = ctx.batch_stats()
     batched = total / (np.median(ms) * 1e-3)
     # plain per-instance kernel on a sample of instances of every job
-    psegs, pms = 0, 0.0
+    psegs, pms, pinst = 0, 0.0, 0
     for j in jobs:
+        if j["profile"] == "lattice":  # the plain kernel covers the single-tube profiles
+            continue
         idx = np.linspace(0, len(j["T"]) - 1, 2).astype(int)
         _, _, _, t = ctx.eval_plain(j["handle"], j["field"], j["cx"][idx], j["cy"][idx],
                                     j["T"][idx], j["F"], j["group"])
-        L = ctx  # noqa: F841
         Nl_ppl = j["segments"] // len(j["T"])
         psegs += Nl_ppl * len(idx)
+        pinst += len(idx)
         pms += t
     plain = psegs / (pms * 1e-3)
     print(json.dumps({
@@ -276,11 +281,12 @@ def run_batch(args):
         "segments_per_step": int(total), "tiles": st["tiles"], "grid": st["grid"],
         "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas},
         "plain_per_instance": {"value": plain, "unit": "segments/s",
-                               "sample_instances": 2 * len(jobs), "device_ms": pms},
+                               "sample_instances": pinst, "device_ms": pms,
+                               "jobs": sum(j["profile"] != "lattice" for j in jobs)},
         "speedup_vs_plain": batched / plain,
         "config": {"workload": "uneven batch drawn as the 512-instance configuration "
-                               "(seed 4), %d jobs, profiles smooth+gaussian, spinor, "
-                               "5 Simpson nodes" % len(jobs),
+                               "(seed 4), %d jobs, profiles %s, spinor, "
+                               "5 Simpson nodes" % (len(jobs), "+".join(profiles)),
                    "ensembles": len(ens)}}))
     ctx.close()
 
@@ -428,22 +434,24 @@ def lattice_image_counts(bbox, cx, cy, T, a, lam, rimage):
 
 def run_lattice(args):
     """Square lattice of Gaussian tubes (lambda = 1, F = 1, images to 12a):
-    Nl = 8192 x ppl = 4096 (seed 3), 96 log-spaced T in [1e-2, 1e2], a 4 x 4
-    grid of centres over one unit cell (the configuration's 32 x 32 grid
-    subsampled to keep the run within minutes), a in {2, 5, 10}, scalar and
-    spinor; one timed evaluation per case after a warm-up."""
+    Nl = 8192 x ppl = 4096 (seed 3), the configuration's 32 x 32 grid of
+    centres over one unit cell at every 12th of its 96 log-spaced T in
+    [1e-2, 1e2] (8 T: the whole grid would take ~10 min per case), a in
+    {2, 5, 10}, scalar and spinor; one timed evaluation per case after a
+    warm-up."""
     import torch
 
     import wltube
 
-    Nl, ppl, seed, nT, ngrid = 8192, 4096, 3, 96, args.lattice_grid
+    Nl, ppl, seed, ngrid = 8192, 4096, 3, args.lattice_grid
     ctx = wltube.Context(0)
     h = ctx.generate(seed, Nl, ppl)
     host = ctx.download(h)
     bbox = np.stack([host[:, :, 0].min(1), host[:, :, 0].max(1),
                      host[:, :, 1].min(1), host[:, :, 1].max(1)], axis=1)
     del host
-    Tg = np.geomspace(1e-2, 1e2, nT)
+    Tg = np.geomspace(1e-2, 1e2, 96)[args.lattice_tstride // 2::args.lattice_tstride]
+    nT = len(Tg)
     stream = torch.cuda.ExternalStream(ctx.stream())
     mufu_peak = ctx.peak_probe(1)
     cases = []
@@ -495,9 +503,10 @@ def run_lattice(args):
                      "peak_mufu_ops_per_s": mufu_peak,
                      "peak_source": "MUFU rcp probe measured in this run"},
         "config": {"workload": "square lattice of Gaussian tubes, lambda=1, F=1, images to "
-                               "|R|<=12a, Nl=8192 x ppl=4096 (seed 3), 96 log T in [1e-2,1e2], "
-                               "%dx%d centres over one unit cell, (a, fermion) in %s, 5 Simpson "
-                               "nodes, exact mode" % (ngrid, ngrid, args.lattice_cases)}}))
+                               "|R|<=12a, Nl=8192 x ppl=4096 (seed 3), %d of the 96 log T in "
+                               "[1e-2,1e2] (every %dth), %dx%d centres over one unit cell, "
+                               "(a, fermion) in %s, 5 Simpson nodes, exact mode"
+                               % (nT, args.lattice_tstride, ngrid, ngrid, args.lattice_cases)}}))
     ctx.release(h)
     ctx.close()
 
@@ -517,9 +526,13 @@ def main():
                     help="c2: the headline spinor workload; batch: uneven multi-job batch; "
                          "serve: Poisson request stream through the server")
     ap.add_argument("--jobs", type=int, default=32, help="jobs of the batch workload")
+    ap.add_argument("--batch-profiles", default="smooth,gaussian",
+                    help="profiles of the batch jobs (add lattice for lattice a = 5 lambda jobs)")
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
-    ap.add_argument("--lattice-grid", type=int, default=4,
+    ap.add_argument("--lattice-grid", type=int, default=32,
                     help="centres per side of the unit cell (lattice workload)")
+    ap.add_argument("--lattice-tstride", type=int, default=12,
+                    help="take every n-th of the 96 proper times (lattice workload)")
     ap.add_argument("--lattice-cases", default="2:0,2:1,5:0,5:1,10:0,10:1",
                     help="a:fermion pairs of the lattice workload")
     ap.add_argument("--serve-profiles", default="smooth,gaussian",

@@ -1,0 +1,114 @@
+"""The benchmark configurations at their full sizes.
+
+The FP64 oracle finishes a few instances of each in seconds; the rest is
+checked through properties that do not depend on size: an instance's result
+does not depend on the other instances of the launch (bit for bit), F = 0
+gives <W> = 1 exactly, and the mean and SEM outputs are the mean and standard
+error of the per-group values.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+W_TOL, W_FLOOR = 1e-5, 1e-2
+
+
+def werr(w, ref, scale):
+    return np.abs(w - ref) / np.maximum(np.abs(ref), W_FLOOR * scale)
+
+
+def f32_exact(cx, cy, T):
+    rt = np.sqrt(np.asarray(T, np.float64)).astype(np.float32).astype(np.float64)
+    return (np.asarray(cx, np.float32).astype(np.float64),
+            np.asarray(cy, np.float32).astype(np.float64), rt * rt)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import wltube
+
+    c = wltube.Context(0)
+    yield c
+    c.close()
+
+
+def test_scalar_configuration_full_size(ctx):
+    """Scalar QED, smooth tube (F = 1, lambda = 1): Nl 1024 x ppl 1024 (seed 1),
+    64 log T in [1e-2, 1e2] x 16 rho in [0, 5], 5 Simpson nodes."""
+    import wltube
+
+    Nl, ppl = 1024, 1024
+    Tg, rho = np.geomspace(1e-2, 1e2, 64), np.linspace(0.0, 5.0, 16)
+    cx, cy, T = f32_exact(np.repeat(rho, 64), np.zeros(1024), np.tile(Tg, 16))
+    fld = wltube.field("smooth", fermion=0, nint=4)
+    h = ctx.generate(1, Nl, ppl)
+    g, mean, sem = ctx.eval(h, fld, cx, cy, T, [1.0, 0.0])
+    # the oracle on 48 instances spread over the grid
+    idx = np.linspace(0, 1023, 48).astype(int)
+    loops = ctx.download(h)
+    ref, S = O.eval_groups(loops, cx[idx], cy[idx], T[idx], [1.0],
+                           O.field("smooth", fermion=0, nint=4), return_scale=True)
+    assert werr(g[idx, :1], ref, S).max() < W_TOL
+    # F = 0: every loop factor is exactly 1
+    assert np.all(g[:, 1] == 1.0)
+    # mean / SEM are those of the groups
+    ng = g.shape[2]
+    np.testing.assert_allclose(mean, g.mean(axis=2), rtol=1e-14, atol=1e-15)
+    np.testing.assert_allclose(sem, g.std(axis=2, ddof=1) / np.sqrt(ng), rtol=1e-9, atol=1e-15)
+    # the same instances in a launch of their own: bit for bit
+    g1, _, _ = ctx.eval(h, fld, cx[idx], cy[idx], T[idx], [1.0, 0.0])
+    assert np.array_equal(g1, g[idx])
+    ctx.release(h)
+
+
+def test_spinor_configuration_full_size(ctx):
+    """Spinor QED, smooth tube, F in {0.1, 1, 10}: Nl 5120 x ppl 2048 (seed 2),
+    128 log T in [1e-3, 1e3] x 64 rho in [0, 8] -- the benchmark workload."""
+    import wltube
+
+    Nl, ppl = 5120, 2048
+    Tg, rho = np.geomspace(1e-3, 1e3, 128), np.linspace(0.0, 8.0, 64)
+    cx, cy, T = f32_exact(np.repeat(rho, 128), np.zeros(8192), np.tile(Tg, 64))
+    F = [0.1, 1.0, 10.0]
+    fld = wltube.field("smooth", fermion=1, nint=4)
+    h = ctx.generate(2, Nl, ppl)
+    g, mean, sem = ctx.eval(h, fld, cx, cy, T, F)
+    assert np.all(np.isfinite(g))
+    # a subset alone: bit for bit
+    sub = np.arange(3, 8192, 97)
+    g1, _, _ = ctx.eval(h, fld, cx[sub], cy[sub], T[sub], F)
+    assert np.array_equal(g1, g[sub])
+    # the oracle on instances with spin exponents below ~25 (T <= 4, F <= 1)
+    pick = [r * 128 + k for r in (0, 16, 63) for k in (0, 30, 55, 64, 72)]
+    loops = ctx.download(h)
+    ref, S = O.eval_groups(loops, cx[pick], cy[pick], T[pick], F[:2],
+                           O.field("smooth", fermion=1, nint=4), return_scale=True)
+    assert np.all(T[pick] <= 4.0)
+    assert werr(g[pick, :2], ref, S).max() < W_TOL
+    ctx.release(h)
+
+
+def test_lattice_configuration_full_ensemble(ctx):
+    """Square lattice of Gaussian tubes (a = 5 lambda, images to 12 a, F = 1):
+    Nl 8192 x ppl 4096 (seed 3), centres over one unit cell, scalar and
+    spinor; the oracle sums the same images in FP64."""
+    import wltube
+
+    Nl, ppl, a = 8192, 4096, 5.0
+    h = ctx.generate(3, Nl, ppl)
+    u = np.array([0.5, 2.5, 4.5])
+    cx, cy, T = f32_exact(np.repeat(u, 16), np.tile(np.repeat(u, 16)[::-1], 1),
+                          np.tile(np.geomspace(1e-2, 1.0, 16), 3))
+    loops = ctx.download(h)
+    for fe in (0, 1):
+        fld = wltube.field("lattice", fermion=fe, nint=4, lambda2=1.0, tubedist=a)
+        g, _, _ = ctx.eval(h, fld, cx, cy, T, [1.0])
+        pick = [0, 15, 24, 47]
+        ref, S = O.eval_groups(loops, cx[pick], cy[pick], T[pick], [1.0],
+                               O.field("lattice", fermion=fe, nint=4, mode=1, lambda2=1.0,
+                                       tubedist=a), return_scale=True)
+        assert werr(g[pick], ref, S).max() < W_TOL, fe
+    ctx.release(h)
