@@ -333,11 +333,14 @@ __device__ __forceinline__ void gauss_q(float x, float &q, float &e) {
 // One segment z_i -> z_j against every image of the range: in units of
 // x = rho^2/lambda^2, the reference's Gaussian Simpson integral per image,
 // exact mode (no clamps).  Adds sum_R (u_R x Delta)/l2 * sum_w q(x) to ph and
-// sum_R sum_w e^-x to sp (the f' scale 1/l2 is applied per loop).
+// sum_R sum_w e^-x to sp (the f' scale 1/l2 is applied per loop).  Not
+// inlined: the image loop with its five node evaluations is large, and one
+// copy of it per call site (a dozen in the sweep) overflowed the instruction
+// cache (ncu: "no instruction" the top stall); returns the updated (ph, sp).
 template <bool FERM, int NINT>
-__device__ __forceinline__ void segment_lattice(float zix, float ziy, float zjx, float zjy,
-                                                const FieldDev &F, const ImgRange &img,
-                                                float &ph, float &sp) {
+__device__ __noinline__ float2 segment_lattice(float zix, float ziy, float zjx, float zjy,
+                                               const FieldDev &F, const ImgRange img,
+                                               float ph, float sp) {
   const float dx = zjx - zix, dy = zjy - ziy;
   const float il2 = F.inv_l2;
   const float cs = fmaf(dx, dx, dy * dy) * il2;
@@ -378,6 +381,7 @@ __device__ __forceinline__ void segment_lattice(float zix, float ziy, float zjx,
       if (FERM) sp += fmaf(4.0f, fo, fmaf(2.0f, fe, e0 + e1));
     }
   }
+  return make_float2(ph, sp);
 }
 
 // the segment of profile P (the image range is used by the lattice only)
@@ -385,10 +389,13 @@ template <int P, bool FERM, int NINT>
 __device__ __forceinline__ void seg(float zix, float ziy, float zjx, float zjy,
                                     const FieldDev &F, const ImgRange &img, float &ph,
                                     float &sp) {
-  if constexpr (P == kLattice)
-    segment_lattice<FERM, NINT>(zix, ziy, zjx, zjy, F, img, ph, sp);
-  else
+  if constexpr (P == kLattice) {
+    const float2 r = segment_lattice<FERM, NINT>(zix, ziy, zjx, zjy, F, img, ph, sp);
+    ph = r.x;
+    sp = r.y;
+  } else {
     segment<P, FERM, NINT>(zix, ziy, zjx, zjy, F, ph, sp);
+  }
 }
 
 // Kahan compensated accumulation: sum - comp is the running total.

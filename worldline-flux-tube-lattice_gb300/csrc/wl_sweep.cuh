@@ -141,7 +141,7 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
         zBx = P2x; zBy = P2y;
         zOx = P3x; zOy = P3y;
       };
-      if constexpr (Profile<P>::kHeavy) {
+      if constexpr (Profile<P>::kHeavy || P == kLattice) {
 #pragma unroll 1
         for (; q < qe; ++q) group(q);
       } else {
