@@ -293,6 +293,79 @@ __device__ __forceinline__ void segment(float zix, float ziy, float zjx, float z
   if (FERM) sp += fmaf(4.0f, fo, fmaf(2.0f, fe, f0 + f1));
 }
 
+// ------------------------------------------------ packed pairs (f32x2) --
+// Two instances per thread: every FP32 operation of the segment runs as one
+// packed fma/add/mul.rn.f32x2 on the pair (each half rounds exactly like the
+// scalar operation), which halves the issue slots of the FP32 work; the MUFU
+// reciprocals and the clamps stay per half.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 max2(float2 a, float b) {
+  return make_float2(fmaxf(a.x, b), fmaxf(a.y, b));
+}
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcp_fast(a.x), rcp_fast(a.y)); }
+
+// the light profiles on a pair: g = f/rho^2 and fp = f'/fp_scale as in eval
+template <int P>
+__device__ __forceinline__ void eval2(float2 r2, const FieldDev &F, float2 &g, float2 &fp) {
+  if constexpr (P == kSmooth) {
+    g = rcp2(r2);
+    fp = mul2(g, g);
+  } else {
+    Profile<P>::eval(r2.x, F, g.x, fp.x);
+    Profile<P>::eval(r2.y, F, g.y, fp.y);
+  }
+}
+
+// segment() on a pair of instances (same loop segment, two centres / T)
+template <int P, bool FERM, int NINT>
+__device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, float2 zjy,
+                                         const FieldDev &F, float2 &ph, float2 &sp) {
+  static_assert(!Profile<P>::kHeavy && NINT > 0, "pairs: light profiles, fixed intervals");
+  const float2 dx = add2(zjx, neg2(zix)), dy = add2(zjy, neg2(ziy));
+  float2 a = fma2(zix, zix, mul2(ziy, ziy));
+  float2 b = fma2(zix, dx, mul2(ziy, dy));
+  float2 c = fma2(dx, dx, mul2(dy, dy));
+  const float2 xyyx = fma2(zix, zjy, neg2(mul2(ziy, zjx)));
+  a = max2(a, F.clampA);
+  b = max2(b, F.clampB);
+  c = max2(c, F.clampC);
+  const float2 b2 = add2(b, b);
+  const float2 as = add2(a, f2(profile_shift<P>(F)));
+  const float2 ae = add2(add2(as, b2), c);
+  float2 g0, f0, g1, f1;
+  eval2<P>(as, F, g0, f0);
+  eval2<P>(ae, F, g1, f1);
+  float2 so = f2(0.0f), se = f2(0.0f), fo = f2(0.0f), fe = f2(0.0f);
+#pragma unroll
+  for (int j = 1; j < NINT; j++) {
+    const float t = (float)j * (1.0f / (float)NINT);
+    const float2 r2 = fma2(fma2(c, f2(t), b2), f2(t), as);
+    float2 g, fp;
+    eval2<P>(r2, F, g, fp);
+    if (j & 1) {
+      so = add2(so, g);
+      if (FERM) fo = add2(fo, fp);
+    } else {
+      se = add2(se, g);
+      if (FERM) fe = add2(fe, fp);
+    }
+  }
+  const float2 S = fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(g0, g1)));
+  ph = fma2(xyyx, S, ph);
+  if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(f0, f1))));
+}
+
+__device__ __forceinline__ void kahan_add2(float2 &sum, float2 &comp, float2 x) {
+  const float2 y = add2(x, neg2(comp));
+  const float2 t = add2(sum, y);
+  comp = add2(add2(t, neg2(sum)), neg2(y));
+  sum = t;
+}
+
 // ---------------------------------------------------------- lattice --
 // Square lattice of Gaussian tubes at R = a(m, n).  Per (loop, instance) the
 // images within rcut of the loop's scaled bounding box (and |R| <= rimage)

@@ -208,6 +208,179 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
   return true;
 }
 
+// The same tile on packed pairs: thread t runs instances t and t + 128 of a
+// tile of kPairTile, every FP32 operation of the segments as one f32x2
+// operation on the pair (each half rounds as the scalar sweep does); the
+// per-loop epilogue runs per half.  Light profiles with a fixed interval count.
+constexpr int kPairTile = 2 * kSweepThreads;
+
+template <int P, bool FERM, int NINT>
+__device__ __forceinline__ bool sweep_tile2(const SweepArgs &A, int tile_x, int chunk,
+                                            uint64_t *full_bar, double (*sacc)[kPairTile],
+                                            int *bad, float4 *ring, int &consumed) {
+  const int tid = threadIdx.x;
+  const int sA = tile_x * kPairTile + tid, sB = sA + kSweepThreads;
+  const bool liveA = sA < A.ninst, liveB = sB < A.ninst;
+  const int iA = liveA ? sA : A.ninst - 1, iB = liveB ? sB : A.ninst - 1;
+  const int l0 = chunk * A.chunk_loops;
+  const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
+  const int K = A.chunk_loops * nck;
+  const float2 cx = make_float2(A.cx[iA], A.cx[iB]), cy = make_float2(A.cy[iA], A.cy[iB]);
+  const float2 s = make_float2(A.rtT[iA], A.rtT[iB]);
+  const FieldDev &F = A.field;
+  const int base = consumed;
+
+  auto issue = [&](int k) {
+    const int st = (base + k) % kSweepStages;
+    const int l = l0 + k / nck, c = k % nck;
+    const int p0 = c * kSweepChunkPts;
+    const int np = min(kSweepChunkPts, A.ppl - p0);
+    const uint32_t bytes = (uint32_t)np * (uint32_t)sizeof(float4);
+    mbar_arrive_expect_tx(&full_bar[st], bytes);
+    bulk_g2s(ring + st * kSweepChunkPts, A.loops + (size_t)l * A.ppl + p0, bytes,
+             &full_bar[st]);
+  };
+  if (tid == 0)
+    for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
+#pragma unroll
+  for (int r = 0; r < kMaxF * 3; ++r) sacc[r][tid] = sacc[r][tid + kSweepThreads] = 0.0;
+
+  float2 ph[3], pc[3], sp[3], sc[3];
+  float2 zAx = f2(0.f), zAy = f2(0.f), zBx = f2(0.f), zBy = f2(0.f), zOx = f2(0.f), zOy = f2(0.f);
+  float2 z0x = f2(0.f), z0y = f2(0.f), z1x = f2(0.f), z1y = f2(0.f), z2x = f2(0.f), z2y = f2(0.f);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) ph[r] = pc[r] = sp[r] = sc[r] = f2(0.f);
+
+  int k = 0;
+  for (; k < K; ++k) {
+    const int st = (base + k) % kSweepStages;
+    const uint32_t par = (uint32_t)((base + k) / kSweepStages) & 1u;
+    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) *bad = 1;
+    const int c = k % nck;
+    const int p0 = c * kSweepChunkPts;
+    const int p1 = min(A.ppl, p0 + kSweepChunkPts);
+    const float2 *pts = reinterpret_cast<const float2 *>(ring + st * kSweepChunkPts);
+    auto pt = [&](int p, float2 &x, float2 &y) {
+      const float2 v = pts[2 * (p - p0)];
+      x = fma2(s, f2(v.x), cx);
+      y = fma2(s, f2(v.y), cy);
+    };
+    int q = p0 >> 2;
+    const int qend = p1 >> 2;
+    if (c == 0) {
+#pragma unroll
+      for (int r = 0; r < 3; ++r) ph[r] = pc[r] = sp[r] = sc[r] = f2(0.f);
+      float2 z3x, z3y;
+      pt(0, z0x, z0y);
+      pt(1, z1x, z1y);
+      pt(2, z2x, z2y);
+      pt(3, z3x, z3y);
+      segment2<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, ph[0], sp[0]);
+      zAx = z0x; zAy = z0y;
+      zBx = z2x; zBy = z2y;
+      zOx = z3x; zOy = z3y;
+      q = 1;
+    }
+    while (q < qend) {
+      const int qe = min(q + 8, qend);
+      float2 bp0 = f2(0.f), bp1 = f2(0.f), bp2 = f2(0.f), bs0 = f2(0.f), bs1 = f2(0.f),
+             bs2 = f2(0.f);
+#pragma unroll 2
+      for (; q < qe; ++q) {
+        float2 P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
+        pt(4 * q, P0x, P0y);
+        pt(4 * q + 1, P1x, P1y);
+        pt(4 * q + 2, P2x, P2y);
+        pt(4 * q + 3, P3x, P3y);
+        segment2<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, bp2, bs2);
+        segment2<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, bp0, bs0);
+        segment2<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, bp1, bs1);
+        segment2<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, bp0, bs0);
+        zAx = P0x; zAy = P0y;
+        zBx = P2x; zBy = P2y;
+        zOx = P3x; zOy = P3y;
+      }
+      kahan_add2(ph[0], pc[0], bp0);
+      kahan_add2(ph[1], pc[1], bp1);
+      kahan_add2(ph[2], pc[2], bp2);
+      if (FERM) {
+        kahan_add2(sp[0], sc[0], bs0);
+        kahan_add2(sp[1], sc[1], bs1);
+        kahan_add2(sp[2], sc[2], bs2);
+      }
+    }
+    if (c == nck - 1) {
+      float2 tp0 = f2(0.f), tp1 = f2(0.f), tp2 = f2(0.f), ts0 = f2(0.f), ts1 = f2(0.f),
+             ts2 = f2(0.f);
+      segment2<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, tp0, ts0);
+      segment2<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, tp1, ts1);
+      segment2<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, tp2, ts2);
+      kahan_add2(ph[0], pc[0], tp0);
+      kahan_add2(ph[1], pc[1], tp1);
+      kahan_add2(ph[2], pc[2], tp2);
+      kahan_add2(sp[0], sc[0], ts0);
+      kahan_add2(sp[1], sc[1], ts1);
+      kahan_add2(sp[2], sc[2], ts2);
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {  // per-loop epilogue of each half
+        auto lane = [h](float2 v) { return h ? v.y : v.x; };
+        const int ih = h ? iB : iA, col = tid + h * kSweepThreads;
+        const df G[3] = {fast_two_sum(lane(ph[0]), -lane(pc[0])),
+                         fast_two_sum(lane(ph[1]), -lane(pc[1])),
+                         fast_two_sum(lane(ph[2]), -lane(pc[2]))};
+        const df H[3] = {fast_two_sum(lane(sp[0]), -lane(sc[0])),
+                         fast_two_sum(lane(sp[1]), -lane(sc[1])),
+                         fast_two_sum(lane(sp[2]), -lane(sc[2]))};
+        const df tq = {A.tqh[ih], A.tql[ih]};
+        loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
+                            [&](int j, double w0, double w1, double w2) {
+                              sacc[3 * j][col] += w0;
+                              sacc[3 * j + 1][col] += w1;
+                              sacc[3 * j + 2][col] += w2;
+                            });
+      }
+    }
+    __syncthreads();
+    if (*bad) break;
+    if (tid == 0 && k + kSweepStages < K) issue(k + kSweepStages);
+  }
+  if (*bad) {
+    if (tid == 0) {
+      const int kend = min(K, k + kSweepStages);
+      for (int kk = k; kk < kend; ++kk)
+        mbar_wait_bounded(&full_bar[(base + kk) % kSweepStages],
+                          (uint32_t)((base + kk) / kSweepStages) & 1u, A.wait_tries);
+      atomicExch(A.status, kDevTimeout);
+    }
+    consumed = base + K;
+    return false;
+  }
+  consumed = base + K;
+  for (int r = 0; r < A.nF * 3; ++r) {
+    double *o = A.partial + ((size_t)chunk * A.nF * 3 + r) * A.ninst;
+    if (liveA) o[iA] = sacc[r][tid];
+    if (liveB) o[iB] = sacc[r][tid + kSweepThreads];
+  }
+  return true;
+}
+
+template <int P, bool FERM, int NINT>
+__global__ void __launch_bounds__(kSweepThreads, 4)
+    sweep2_kernel(const __grid_constant__ SweepArgs A) {
+  extern __shared__ __align__(128) float4 ring[];
+  __shared__ __align__(8) uint64_t full_bar[kSweepStages];
+  __shared__ int sm_bad;
+  __shared__ double sacc[kMaxF * 3][kPairTile];
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kSweepStages; ++st) mbar_init(&full_bar[st], 1);
+    fence_mbar_init();
+    sm_bad = 0;
+  }
+  __syncthreads();
+  int consumed = 0;
+  sweep_tile2<P, FERM, NINT>(A, blockIdx.x, blockIdx.y, full_bar, sacc, &sm_bad, ring, consumed);
+}
+
 template <int P, bool FERM, int NINT>
 __global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweepMinBlocks)
     sweep_kernel(const __grid_constant__ SweepArgs A) {
@@ -298,6 +471,16 @@ template <int P>
 cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStream_t s) {
   const dim3 grid((a.ninst + kSweepThreads - 1) / kSweepThreads, a.n_chunks);
   const size_t smem = sweep_smem_bytes();
+  if constexpr (P == kSmooth) {  // packed pairs
+    const dim3 grid2((a.ninst + kPairTile - 1) / kPairTile, a.n_chunks);
+    if (nint == 4) {
+      if (fermion)
+        sweep2_kernel<P, true, 4><<<grid2, kSweepThreads, smem, s>>>(a);
+      else
+        sweep2_kernel<P, false, 4><<<grid2, kSweepThreads, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
 #define WL_SWEEP_CASE(FE, NI)                                                      \
   if (fermion == FE && (NI == 0 || nint == NI)) {                                  \
     sweep_kernel<P, FE, NI><<<grid, kSweepThreads, smem, s>>>(a);                  \
