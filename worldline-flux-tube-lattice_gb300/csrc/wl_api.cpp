@@ -433,8 +433,9 @@ int batch_plan(wl_ctx *ctx, int njobs, const wl_job *jobs, int points, BatchPlan
     rj.first = P->flat_total;
     rj.out_group = (double *)(uintptr_t)(out_off[i]);
     P->flat_total += n * J.nF;
-    const int tiles_x = (n + wl::kSweepThreads - 1) / wl::kSweepThreads;
-    const int cost = lcs[i] * e.ppl;
+    const int per_tile = wl::sweep_tile_instances(kprofs[i], J.field.nint);
+    const int tiles_x = (n + per_tile - 1) / per_tile;
+    const int cost = lcs[i] * e.ppl * (per_tile / wl::kSweepThreads);
     for (int c = 0; c < a.n_chunks; ++c)
       for (int t = 0; t < tiles_x; ++t) P->tiles.push_back({i, t, c, cost});
   }

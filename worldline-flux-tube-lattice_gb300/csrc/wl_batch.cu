@@ -14,9 +14,32 @@ namespace wl {
 
 namespace {
 
+// One tile of a job: packed pairs (256 instances) for the light profiles at 4
+// intervals, one instance per thread otherwise -- the split the single-job
+// sweep makes (sweep_pairs), so a job's results match it bit for bit.
 template <bool FERM, int NINT>
 __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, int chunk,
-                                         const SweepShared &S, int &consumed) {
+                                         const SweepShared &S, double (*sacc2)[kPairTile],
+                                         int &consumed) {
+  if constexpr (NINT == 4) {
+    switch (kprof) {
+      case kSmooth:
+        sweep_tile2<kSmooth, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring, consumed);
+        return;
+      case kGaussian:
+        sweep_tile2<kGaussian, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
+                                        consumed);
+        return;
+      case kStep:
+        sweep_tile2<kStep, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring, consumed);
+        return;
+      case kQuadratic:
+        sweep_tile2<kQuadratic, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
+                                         consumed);
+        return;
+      default: break;
+    }
+  }
   switch (kprof) {
     case kSmooth: sweep_tile<kSmooth, FERM, NINT>(A, tx, chunk, S, consumed); break;
     case kGaussian: sweep_tile<kGaussian, FERM, NINT>(A, tx, chunk, S, consumed); break;
@@ -27,17 +50,20 @@ __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, 
   }
 }
 
-constexpr int kBatchMinBlocks = 5;
+constexpr int kBatchMinBlocks = 4;
 
 __global__ void __launch_bounds__(kSweepThreads, kBatchMinBlocks)
     batch_kernel(const __grid_constant__ BatchArgs B) {
   extern __shared__ __align__(128) float4 ring[];
   __shared__ __align__(8) uint64_t full_bar[kSweepStages];
   __shared__ int sm_bad;
-  __shared__ double sacc[kMaxF * 3][kSweepThreads];
+  // FP64 W - 1 sums: [kMaxF * 3][kPairTile] for pair tiles, the first
+  // [kMaxF * 3][kSweepThreads] of it for one-instance tiles
+  __shared__ double sacc2[kMaxF * 3][kPairTile];
   __shared__ __align__(16) SweepArgs job;
   __shared__ int cur[4];
-  const SweepShared S = {full_bar, sacc, &sm_bad, ring};
+  const SweepShared S = {full_bar, reinterpret_cast<double(*)[kSweepThreads]>(&sacc2[0][0]),
+                         &sm_bad, ring};
   sweep_shared_init(S);
   int consumed = 0;
   for (;;) {
@@ -64,14 +90,14 @@ __global__ void __launch_bounds__(kSweepThreads, kBatchMinBlocks)
     const int tx = cur[2], chunk = cur[3];
     if (job.fermion) {
       if (job.nint == 4)
-        run_tile<true, 4>(job.kprof, job, tx, chunk, S, consumed);
+        run_tile<true, 4>(job.kprof, job, tx, chunk, S, sacc2, consumed);
       else
-        run_tile<true, 0>(job.kprof, job, tx, chunk, S, consumed);
+        run_tile<true, 0>(job.kprof, job, tx, chunk, S, sacc2, consumed);
     } else {
       if (job.nint == 4)
-        run_tile<false, 4>(job.kprof, job, tx, chunk, S, consumed);
+        run_tile<false, 4>(job.kprof, job, tx, chunk, S, sacc2, consumed);
       else
-        run_tile<false, 0>(job.kprof, job, tx, chunk, S, consumed);
+        run_tile<false, 0>(job.kprof, job, tx, chunk, S, sacc2, consumed);
     }
     if (sm_bad) break;  // a copy timed out: the status is set, stop taking tiles
     __syncthreads();    // cur[] and job are rewritten next

@@ -314,6 +314,21 @@ __device__ __forceinline__ void eval2(float2 r2, const FieldDev &F, float2 &g, f
   if constexpr (P == kSmooth) {
     g = rcp2(r2);
     fp = mul2(g, g);
+  } else if constexpr (P == kGaussian) {  // as Profile<kGaussian>::eval, per half
+    const float2 x = mul2(r2, f2(F.inv_l2));
+    const float2 a = mul2(x, f2(-1.4426950408889634f));
+    const float2 e = make_float2(ex2_fast(a.x), ex2_fast(a.y));
+    // the small-x polynomial of one_minus_expneg_over_x, on the pair
+    float2 p = f2(-0.0011216341517865658f);
+    p = fma2(p, x, f2(0.008187385275959969f));
+    p = fma2(p, x, f2(-0.041629087179899216f));
+    p = fma2(p, x, f2(0.16666224598884583f));
+    p = fma2(p, x, f2(-0.4999998211860657f));
+    p = fma2(p, x, f2(1.0f));
+    const float2 sm = mul2(p, f2(F.inv_l2));
+    const float2 bg = mul2(add2(f2(1.0f), neg2(e)), rcp2(r2));
+    g = make_float2(x.x < 0.5f ? sm.x : bg.x, x.y < 0.5f ? sm.y : bg.y);
+    fp = e;
   } else {
     Profile<P>::eval(r2.x, F, g.x, fp.x);
     Profile<P>::eval(r2.y, F, g.y, fp.y);

@@ -49,6 +49,17 @@ struct SweepArgs {
   const int *perm;
 };
 
+// Instances per tile of the sweep: the light profiles at 4 Simpson intervals
+// run two instances per thread as packed f32x2 pairs (256 per CTA of 128
+// threads), everything else one per thread.
+inline __host__ __device__ bool sweep_pairs(int kprof, int nint) {
+  return nint == 4 &&
+         (kprof == kSmooth || kprof == kStep || kprof == kQuadratic || kprof == kGaussian);
+}
+inline __host__ __device__ int sweep_tile_instances(int kprof, int nint) {
+  return sweep_pairs(kprof, nint) ? 2 * kSweepThreads : kSweepThreads;
+}
+
 // Persistent multi-job sweep: a queue of tiles (job, instance tile, loop
 // chunk) drained by one CTA per slot; jobs differ in ensemble, profile,
 // instances, flux values and loops per tile.

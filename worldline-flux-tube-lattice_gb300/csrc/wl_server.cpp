@@ -220,9 +220,10 @@ int check_request(wl_server *s, const wl_request *q, Req *R) {
   R->ng = ng;
   R->lc = wl::rt_loops_per_tile(s->cfg.points_per_tile, q->ppl, q->group);
   R->n_chunks = q->Nl / R->lc;
-  R->tiles_x = (n + wl::kSweepThreads - 1) / wl::kSweepThreads;
+  const int per_tile = wl::sweep_tile_instances(R->kprof, q->field.nint);
+  R->tiles_x = (n + per_tile - 1) / per_tile;
   R->ntiles = (long long)R->n_chunks * R->tiles_x;
-  R->tile_work = (double)R->lc * q->ppl * wl::kSweepThreads *
+  R->tile_work = (double)R->lc * q->ppl * per_tile *
                  profile_weight(R->kprof, q->field.fermion != 0);
   R->segments = (double)n * q->Nl * q->ppl;
   const size_t n_part = (size_t)R->n_chunks * nF * 3 * n;
@@ -561,7 +562,8 @@ void launch_quantum(wl_server *s, int k) {
   wl::BatchTile *h = s->h_tiles[k];
   for (size_t i = 0; i < m && n < kMaxQuantumTiles; ++i) {
     Req *R = act[i];
-    const int cost = R->lc * R->q.ppl;
+    const int cost = R->lc * R->q.ppl *
+                     (wl::sweep_tile_instances(R->kprof, R->q.field.nint) / wl::kSweepThreads);
     for (long long c = 0; c < take[i] && n < kMaxQuantumTiles; ++c) {
       const long long t = R->next_tile++;
       h[n++] = {R->slot, (int)(t % R->tiles_x), (int)(t / R->tiles_x), cost};

@@ -471,9 +471,9 @@ template <int P>
 cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStream_t s) {
   const dim3 grid((a.ninst + kSweepThreads - 1) / kSweepThreads, a.n_chunks);
   const size_t smem = sweep_smem_bytes();
-  if constexpr (P == kSmooth) {  // packed pairs
+  if constexpr (P == kSmooth || P == kStep || P == kQuadratic || P == kGaussian) {
     const dim3 grid2((a.ninst + kPairTile - 1) / kPairTile, a.n_chunks);
-    if (nint == 4) {
+    if (sweep_pairs(P, nint)) {  // packed pairs
       if (fermion)
         sweep2_kernel<P, true, 4><<<grid2, kSweepThreads, smem, s>>>(a);
       else
