@@ -498,8 +498,9 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
   WL_CHECK(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
   for (int i = 0; i < njobs; ++i)  // lattice jobs: instances in decreasing proper time
     if (P.jobs[i].perm)
-      WL_CHECK(ctx, wl::launch_order_by_T(P.jobs[i].rtT, P.jobs[i].ninst,
-                                          const_cast<int *>(P.jobs[i].perm), ctx->stream));
+      WL_CHECK(ctx, wl::launch_order_instances(P.jobs[i].cx, P.jobs[i].cy, P.jobs[i].rtT,
+                                               P.jobs[i].ninst, 1.0f / P.jobs[i].field.a,
+                                               const_cast<int *>(P.jobs[i].perm), ctx->stream));
   WL_CHECK(ctx, cudaStreamSynchronize(ctx->stream));  // host vectors are released on return
 
   wl::BatchArgs B;
@@ -849,7 +850,8 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
         cudaGetLastError();
         return fail(ctx, WL_ERR_NOMEM, "cannot allocate the instance order");
       }
-      WL_CHECK(ctx, wl::launch_order_by_T(a.rtT, ninst, ctx->perm.p, ctx->stream));
+      WL_CHECK(ctx, wl::launch_order_instances(a.cx, a.cy, a.rtT, ninst, 1.0f / fd.a,
+                                               ctx->perm.p, ctx->stream));
       a.perm = ctx->perm.p;
     }
     WL_CHECK(ctx, wl::launch_sweep(kprof, fermion, nint, a, ctx->stream));

@@ -418,6 +418,20 @@ __device__ __forceinline__ void gauss_q(float x, float &q, float &e) {
   q = x < 0.5f ? small : big;
 }
 
+// gauss_q on a pair (each half as gauss_q)
+__device__ __forceinline__ void gauss_q2(float2 x, float2 &q, float2 &e) {
+  const float2 a = mul2(f2(-1.4426950408889634f), x);
+  e = make_float2(ex2_fast(a.x), ex2_fast(a.y));
+  const float2 big = mul2(add2(f2(1.0f), neg2(e)), rcp2(x));
+  float2 p = f2(-0.0011216341517865658f);
+  p = fma2(p, x, f2(0.008187385275959969f));
+  p = fma2(p, x, f2(-0.041629087179899216f));
+  p = fma2(p, x, f2(0.16666224598884583f));
+  p = fma2(p, x, f2(-0.4999998211860657f));
+  p = fma2(p, x, f2(1.0f));
+  q = make_float2(x.x < 0.5f ? p.x : big.x, x.y < 0.5f ? p.y : big.y);
+}
+
 // One segment z_i -> z_j against every image of the range: in units of
 // x = rho^2/lambda^2, the reference's Gaussian Simpson integral per image,
 // exact mode (no clamps).  Adds sum_R (u_R x Delta)/l2 * sum_w q(x) to ph and
@@ -437,8 +451,49 @@ __device__ __noinline__ float2 segment_lattice(float zix, float ziy, float zjx, 
   for (int m = img.m0; m <= img.m1; ++m) {
     const float ux = fmaf(-(float)m, F.a, zix);
     const float mm = (float)(m * m);
-    for (int n = img.n0; n <= img.n1; ++n) {
-      if (mm + (float)(n * n) > F.rimg2) continue;
+    // this row's images inside the disk m^2 + n^2 <= (rimage/a)^2 (an interval)
+    int lo = img.n0, hi = img.n1;
+    while (lo <= hi && mm + (float)(lo * lo) > F.rimg2) ++lo;
+    while (hi >= lo && mm + (float)(hi * hi) > F.rimg2) --hi;
+    int n = lo;
+    if constexpr (NINT > 0) {
+      // two images per step as packed pairs: every FP32 operation of the two
+      // images is one f32x2 operation (each half rounds as the single-image
+      // code below) and the sums are added in image order
+      for (; n < hi; n += 2) {
+        const float2 uy = make_float2(fmaf(-(float)n, F.a, ziy), fmaf(-(float)(n + 1), F.a, ziy));
+        const float2 ux2 = f2(ux), dx2 = f2(dx), dy2 = f2(dy), il22 = f2(il2);
+        const float2 as = mul2(fma2(ux2, ux2, mul2(uy, uy)), il22);
+        const float2 bs2 = mul2(mul2(f2(2.0f), fma2(ux2, dx2, mul2(uy, dy2))), il22);
+        const float2 cross = mul2(fma2(ux2, dy2, neg2(mul2(uy, dx2))), il22);
+        float2 q0, e0, q1, e1;
+        gauss_q2(as, q0, e0);
+        gauss_q2(add2(add2(as, bs2), f2(cs)), q1, e1);
+        float2 so = f2(0.f), se = f2(0.f), fo = f2(0.f), fe = f2(0.f);
+#pragma unroll
+        for (int j = 1; j < NINT; j++) {
+          const float t = (float)j * (1.0f / (float)NINT);
+          float2 q, e;
+          gauss_q2(fma2(fma2(f2(cs), f2(t), bs2), f2(t), as), q, e);
+          if (j & 1) {
+            so = add2(so, q);
+            if (FERM) fo = add2(fo, e);
+          } else {
+            se = add2(se, q);
+            if (FERM) fe = add2(fe, e);
+          }
+        }
+        const float2 S = fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(q0, q1)));
+        ph = fmaf(cross.x, S.x, ph);
+        ph = fmaf(cross.y, S.y, ph);
+        if (FERM) {
+          const float2 SP = fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(e0, e1)));
+          sp += SP.x;
+          sp += SP.y;
+        }
+      }
+    }
+    for (; n <= hi; ++n) {
       const float uy = fmaf(-(float)n, F.a, ziy);
       const float as = fmaf(ux, ux, uy * uy) * il2;
       const float bs2 = 2.0f * fmaf(ux, dx, uy * dy) * il2;

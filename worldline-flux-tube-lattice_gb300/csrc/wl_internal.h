@@ -152,9 +152,11 @@ struct TintArgs {
 };
 cudaError_t launch_tint(const TintArgs &a, cudaStream_t s);
 
-// perm[0..n) = instances in decreasing rtT (one CTA, bucketed by log2 rtT;
-// the order inside a bucket is arbitrary and changes no result)
-cudaError_t launch_order_by_T(const float *rtT, int n, int *perm, cudaStream_t s);
+// perm[0..n) = instances in decreasing rtT, then by the centre's position in
+// its lattice cell (one CTA, bucketed; the order inside a bucket is arbitrary
+// and changes no result)
+cudaError_t launch_order_instances(const float *cx, const float *cy, const float *rtT, int n,
+                                   float inv_a, int *perm, cudaStream_t s);
 
 // per-loop bounding boxes of an ensemble (lattice image selection)
 cudaError_t launch_loop_bbox(const float4 *loops, int Nl, int ppl, float4 *out, cudaStream_t s);

@@ -88,36 +88,64 @@ __global__ void group_reduce_kernel(const double *__restrict__ partial, int n_ch
 }
 
 // ------------------------------------------------ lattice instance order --
-constexpr int kOrderBuckets = 512;  // log2(rtT) in steps of 1/16 over [-16, 16)
+// Key: proper time first (log2 rtT in steps of 1/8 over [-16, 16), largest
+// first), then the centre's position in its lattice cell (4 x 4 bins): the
+// number of images an instance sums follows both, so neighbouring threads
+// get similar counts.
+constexpr int kOrderTBins = 256, kOrderCellBins = 16;
+constexpr int kOrderBuckets = kOrderTBins * kOrderCellBins;
 
-__device__ __forceinline__ int order_bucket(float rtT) {
-  const float x = log2f(fmaxf(rtT, 1e-30f)) * 16.0f;
-  const int b = min(max((int)floorf(x) + kOrderBuckets / 2, 0), kOrderBuckets - 1);
-  return kOrderBuckets - 1 - b;  // largest proper times first
+__device__ __forceinline__ int order_bucket(float cx, float cy, float rtT, float inv_a) {
+  const float x = log2f(fmaxf(rtT, 1e-30f)) * 8.0f;
+  const int tb = kOrderTBins - 1 - min(max((int)floorf(x) + kOrderTBins / 2, 0), kOrderTBins - 1);
+  const float u = cx * inv_a, v = cy * inv_a;
+  const int bu = min(max((int)((u - floorf(u)) * 4.0f), 0), 3);
+  const int bv = min(max((int)((v - floorf(v)) * 4.0f), 0), 3);
+  return tb * kOrderCellBins + bu * 4 + bv;
 }
 
-__global__ void __launch_bounds__(1024) order_by_T_kernel(const float *__restrict__ rtT, int n,
-                                                          int *__restrict__ perm) {
+__global__ void __launch_bounds__(1024)
+    order_instances_kernel(const float *__restrict__ cx, const float *__restrict__ cy,
+                           const float *__restrict__ rtT, int n, float inv_a,
+                           int *__restrict__ perm) {
   __shared__ int cnt[kOrderBuckets];
+  __shared__ int part[1024];
   for (int b = threadIdx.x; b < kOrderBuckets; b += blockDim.x) cnt[b] = 0;
   __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&cnt[order_bucket(rtT[i])], 1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    atomicAdd(&cnt[order_bucket(cx[i], cy[i], rtT[i], inv_a)], 1);
+  __syncthreads();
+  // exclusive scan of the counts: each thread scans 4 buckets, then the
+  // thread totals are scanned serially by one thread
+  constexpr int per = kOrderBuckets / 1024;
+  const int b0 = threadIdx.x * per;
+  int tot = 0;
+  for (int b = b0; b < b0 + per; ++b) tot += cnt[b];
+  part[threadIdx.x] = tot;
   __syncthreads();
   if (threadIdx.x == 0) {
     int run = 0;
-    for (int b = 0; b < kOrderBuckets; ++b) {
-      const int c = cnt[b];
-      cnt[b] = run;
+    for (int t = 0; t < 1024; ++t) {
+      const int c = part[t];
+      part[t] = run;
       run += c;
     }
   }
   __syncthreads();
+  int run = part[threadIdx.x];
+  for (int b = b0; b < b0 + per; ++b) {
+    const int c = cnt[b];
+    cnt[b] = run;
+    run += c;
+  }
+  __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x)
-    perm[atomicAdd(&cnt[order_bucket(rtT[i])], 1)] = i;
+    perm[atomicAdd(&cnt[order_bucket(cx[i], cy[i], rtT[i], inv_a)], 1)] = i;
 }
 
-cudaError_t launch_order_by_T(const float *rtT, int n, int *perm, cudaStream_t s) {
-  order_by_T_kernel<<<1, 1024, 0, s>>>(rtT, n, perm);
+cudaError_t launch_order_instances(const float *cx, const float *cy, const float *rtT, int n,
+                                   float inv_a, int *perm, cudaStream_t s) {
+  order_instances_kernel<<<1, 1024, 0, s>>>(cx, cy, rtT, n, inv_a, perm);
   return cudaGetLastError();
 }
 

@@ -493,7 +493,9 @@ bool admit(wl_server *s) {
     ck(cudaMemcpyAsync(dmem + R->o_rj, pin + R->p_rj, R->o_perm - R->o_rj,
                        cudaMemcpyHostToDevice, s->cs), "request upload");
     if (a.perm)  // lattice: instances in decreasing proper time
-      ck(wl::launch_order_by_T(a.rtT, n, const_cast<int *>(a.perm), s->cs), "instance order");
+      ck(wl::launch_order_instances(a.cx, a.cy, a.rtT, n, 1.0f / a.field.a,
+                                    const_cast<int *>(a.perm), s->cs),
+         "instance order");
     if (R->n_aux_in)
       ck(cudaMemcpyAsync(dmem + R->o_aux, pin + R->p_aux, sizeof(double) * R->n_aux_in,
                          cudaMemcpyHostToDevice, s->cs), "grid upload");

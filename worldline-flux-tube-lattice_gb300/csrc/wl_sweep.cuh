@@ -382,7 +382,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
 }
 
 template <int P, bool FERM, int NINT>
-__global__ void __launch_bounds__(kSweepThreads, Profile<P>::kHeavy ? 4 : kSweepMinBlocks)
+__global__ void __launch_bounds__(kSweepThreads,
+                                  (Profile<P>::kHeavy || P == kLattice) ? 4 : kSweepMinBlocks)
     sweep_kernel(const __grid_constant__ SweepArgs A) {
   extern __shared__ __align__(128) float4 ring[];  // [kSweepStages][kSweepChunkPts]
   __shared__ __align__(8) uint64_t full_bar[kSweepStages];
