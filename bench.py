@@ -163,16 +163,20 @@ def cpu_sample(seconds_target=12.0, threads=0):
                        fp32=True, nthreads=threads)
     dt = time.perf_counter() - t0
     rate = 16 * 128 * PPL / dt
-    n = int(max(16, min(len(T), seconds_target * rate / (128 * PPL))))
+    units = seconds_target * rate / PPL          # (instance, loop) pairs in the target time
+    n = int(max(16, min(len(T), units / 128)))
+    nl = int(min(NL, max(128, 128 * round(units / n / 128))))  # more loops once all instances
+    if nl > len(loops):
+        loops = oracle.vloops(SEED, nl, PPL)
     idx = rng.choice(len(T), n, replace=False)
     t0 = time.perf_counter()
-    oracle.eval_groups(loops[:128], cx[idx], cy[idx], T[idx], FLUX, fld, group=128,
+    oracle.eval_groups(loops[:nl], cx[idx], cy[idx], T[idx], FLUX, fld, group=128,
                        fp32=True, nthreads=threads)
     dt = time.perf_counter() - t0
-    segs = n * 128 * PPL
+    segs = n * nl * PPL
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     return segs / dt, cores, "%d loops x %d points x %d (rho,T) instances (3 F each), %.1f s" % (
-        128, PPL, n, dt)
+        nl, PPL, n, dt)
 
 
 def run_reference(args, world, rank):

@@ -135,6 +135,23 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
             int nT, const double *host_T, int nF, const double *host_F, int group, int nbins,
             double *out_leff, double *out_err, double *out_igrand);
 
+/* The effective action per unit length (EffAct.c:83-306): the radial
+ * integral of rho I_g(rho) with I_g the proper-time integral of wl_tint (flux
+ * F, log-spaced T grid), per group g, divided by 4 pi (spinor) or -2 pi
+ * (scalar).  Isolated profiles integrate rho over [0, inf) through
+ * rho = (1 - t)/t with nrho Simpson panels in t (EffAct.c:140-210); periodic
+ * and fixflux over [0, a/2] with 2 nrho intervals (EffAct.c:83-138).  In
+ * WL_MODE_REFCOMPAT the two rules keep the reference's weights (each t panel
+ * evaluates its right end twice; on [0, a/2] the end a/2 is counted twice
+ * and the weights 2 and 4 sit on the opposite points of Simpson's rule); in
+ * WL_MODE_EXACT they are Simpson's rule.  Outputs the mean over groups and
+ * its standard error, optionally the profile's classical action
+ * (EffAct.c:228-279; NaN for the lattice) and the per-group values [Nl/group].
+ * No counterpart as one call in the reference, which runs it as its main(). */
+int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F, int nT,
+                        const double *host_T, int group, int nrho, double *out_action,
+                        double *out_err, double *out_classical, double *out_groups);
+
 /* Asynchronous variant on the context's stream for device-resident inputs and
  * outputs: dev_cx, dev_cy, dev_T [ninst] and the outputs are device pointers
  * (FP64, same layouts as wl_eval; outputs may be NULL), host_F stays a host

@@ -81,3 +81,60 @@ def test_tint_rejects_non_log_grid():
         with pytest.raises(wltube.WlError):
             ctx.tint(h, wltube.field("smooth"), [0.0], [0.1, 0.2, 0.4, 0.5], [1.0], nbins=2)
         ctx.release(h)
+
+
+def rho_rule(profile_cell, nrho, a, ref):
+    """Nodes and weights of the radial integral of rho I(rho) as
+    wl_effective_action documents them (EffAct.c:83-210)."""
+    if profile_cell:
+        n = 2 * nrho
+        h = a / (2.0 * n)
+        rho = h * np.arange(n + 1)
+        if ref:
+            w = np.array([1.0] + [2.0 if (k - 1) % 2 == 0 else 4.0 for k in range(1, n + 1)])
+            w[n] += 1.0
+        else:
+            w = np.array([1.0] + [4.0 if k % 2 else 2.0 for k in range(1, n)] + [1.0])
+        return rho, w * h / 3.0
+    h = 1.0 / nrho
+    wt = np.zeros(2 * nrho + 1)
+    for i in range(nrho):
+        if ref:
+            wt[2 * i + 2] += 2 * h / 6
+        else:
+            wt[2 * i] += h / 6
+            wt[2 * i + 2] += h / 6
+        wt[2 * i + 1] += 4 * h / 6
+    t = 0.5 * h * np.arange(1, 2 * nrho + 1)
+    return (1 - t) / t, wt[1:] / t ** 2
+
+
+@pytest.mark.parametrize("prof,fermion,mode", [("smooth", 1, 0), ("smooth", 0, 1),
+                                               ("fixflux", 0, 0)])
+def test_effective_action_matches_oracle(prof, fermion, mode):
+    import wltube
+
+    loops = O.vloops(9, 512, 128)
+    T = np.exp(np.linspace(np.log(1e-2), np.log(30.0), 17))
+    a, nrho, F = 2.0, 3, 1.0
+    fld = wltube.field(prof, fermion=fermion, nint=4, mode=mode, tubedist=a, lambda2=0.5)
+    with wltube.Context(0) as ctx:
+        h = ctx.upload(loops)
+        act, err, ca, groups = ctx.effective_action(h, fld, F, T, group=128, nrho=nrho)
+        ctx.release(h)
+    rho, w = rho_rule(prof == "fixflux", nrho, a, mode == 0)
+    rho = rho.astype(np.float32).astype(np.float64)  # the kernel's float centre
+    rtf = np.sqrt(T).astype(np.float32).astype(np.float64)
+    ofld = O.field(prof, fermion=fermion, nint=4, mode=mode, tubedist=a, lambda2=0.5)
+    _, _, ig = oracle_tint(loops, rho, rtf * rtf, [F], ofld, 2)
+    I = np.einsum("rjkg,k->rg", ig, log_simpson_weights(T))         # [rho][group]
+    norm = 1 / (4 * np.pi) if fermion else -1 / (2 * np.pi)
+    ref_g = norm * np.einsum("r,r,rg->g", w, rho, np.where(np.isinf(I), 0.0, I))
+    ref = ref_g.mean()
+    ref_se = ref_g.std(ddof=1) / np.sqrt(len(ref_g))
+    assert np.isfinite(act) and err > 0
+    assert abs(act - ref) <= 0.05 * ref_se + 1e-12
+    np.testing.assert_allclose(groups, ref_g, rtol=0, atol=0.05 * ref_se + 1e-12)
+    if prof == "smooth":
+        e = 0.30282212
+        assert np.isclose(ca, -2 * np.pi * F * F / (3 * 0.5 * e * e))

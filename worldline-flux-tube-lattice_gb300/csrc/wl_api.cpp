@@ -1006,12 +1006,14 @@ static void log_simpson_weights(const double *T, int n, double du, double *w) {
   for (int k = 0; k < n; ++k) w[k] *= T[k];
 }
 
-int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const double *host_rho,
-            int nT, const double *host_T, int nF, const double *host_F, int group, int nbins,
-            double *out_leff, double *out_err, double *out_igrand) {
-  if (!ctx) return WL_ERR_INVALID;
-  if (!host_rho || !host_T || !out_leff || !out_err)
-    return fail(ctx, WL_ERR_INVALID, "NULL rho, T or output array");
+// <W> on the (rho, log T) grid, the FP64 proper-time integral per group and
+// the jackknife on the device; results stay there (*ta), the caller copies
+// what it needs and checks the status.
+static int tint_run(wl_ctx *ctx, int handle, const wl_field *field, int nrho,
+                    const double *host_rho, int nT, const double *host_T, int nF,
+                    const double *host_F, int group, int nbins, bool want_igrand,
+                    wl::TintArgs *ta_out) {
+  if (!host_rho || !host_T) return fail(ctx, WL_ERR_INVALID, "NULL rho or T array");
   if (nrho < 1 || nT < 3) return fail(ctx, WL_ERR_INVALID, "need nrho >= 1 and nT >= 3");
   const double du = log(host_T[1]) - log(host_T[0]);
   for (int k = 0; k < nT; ++k) {
@@ -1051,7 +1053,7 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
     return r;
   // aux: rho | T | w | F | Ig | leff | err | igrand
   const size_t n_ig = (size_t)nrho * nF * ng, n_le = (size_t)nrho * nF;
-  const size_t n_igr = out_igrand ? (size_t)nrho * nF * nT * ng : 0;
+  const size_t n_igr = want_igrand ? (size_t)nrho * nF * nT * ng : 0;
   const size_t naux = (size_t)nrho + 2 * (size_t)nT + nF + n_ig + 2 * n_le + n_igr;
   if (ctx->aux.reserve(naux) != cudaSuccess) {
     cudaGetLastError();
@@ -1064,7 +1066,7 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
   memcpy(h.data() + nrho + 2 * nT, host_F, sizeof(double) * nF);
   WL_CHECK(ctx, cudaMemcpyAsync(ctx->aux.p, h.data(), sizeof(double) * h.size(),
                                 cudaMemcpyHostToDevice, ctx->stream));
-  wl::TintArgs ta;
+  wl::TintArgs &ta = *ta_out;
   memset(&ta, 0, sizeof(ta));
   double *d = ctx->aux.p;
   ta.groups = dg;
@@ -1075,7 +1077,7 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
   ta.Ig = d + nrho + 2 * nT + nF;
   ta.leff = ta.Ig + n_ig;
   ta.err = ta.leff + n_le;
-  ta.igrand = out_igrand ? ta.err + n_le : nullptr;
+  ta.igrand = want_igrand ? ta.err + n_le : nullptr;
   ta.nrho = nrho;
   ta.nT = nT;
   ta.nF = nF;
@@ -1092,6 +1094,19 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
   ta.e = 0.30282212;   // Integrand.c:14
   WL_CHECK(ctx, wl::launch_tint(ta, ctx->stream));
   ctx->last_launches = 4;
+  return WL_OK;
+}
+
+int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const double *host_rho,
+            int nT, const double *host_T, int nF, const double *host_F, int group, int nbins,
+            double *out_leff, double *out_err, double *out_igrand) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (!out_leff || !out_err) return fail(ctx, WL_ERR_INVALID, "NULL output array");
+  wl::TintArgs ta;
+  int r = tint_run(ctx, handle, field, nrho, host_rho, nT, host_T, nF, host_F, group, nbins,
+                   out_igrand != nullptr, &ta);
+  if (r) return r;
+  const size_t n_le = (size_t)nrho * nF, n_igr = (size_t)nrho * nF * nT * ta.ng;
   WL_CHECK(ctx, cudaMemcpyAsync(out_leff, ta.leff, sizeof(double) * n_le, cudaMemcpyDeviceToHost,
                                 ctx->stream));
   WL_CHECK(ctx, cudaMemcpyAsync(out_err, ta.err, sizeof(double) * n_le, cudaMemcpyDeviceToHost,
@@ -1100,6 +1115,120 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
     WL_CHECK(ctx, cudaMemcpyAsync(out_igrand, ta.igrand, sizeof(double) * n_igr,
                                   cudaMemcpyDeviceToHost, ctx->stream));
   return check_status(ctx);
+}
+
+// Classical action of the profile (EffAct.c:228-279), e = 0.30282212.
+static double classical_action(int profile, double F, double l2, double a, double lmin) {
+  const double e = 0.30282212, pi = M_PI;
+  switch (profile) {
+    case WL_PROFILE_STEP: return -2.0 * pi * F * F / (e * e * l2);
+    case WL_PROFILE_SMOOTH: return -2.0 * pi * F * F / (3.0 * l2 * e * e);
+    case WL_PROFILE_QUADRATIC: return -8.0 * pi * F * F / (3.0 * l2 * e * e);
+    case WL_PROFILE_GAUSSIAN: return -pi * F * F / (l2 * e * e);
+    case WL_PROFILE_PERIODIC: {  // EffAct.c:228-240 (the reference drops F here)
+      const double l = sqrt(l2), q = 1.0 + exp(a / l);
+      const double pca = 2.0 * a + 4.0 * a / (q * q * q) - l + 4.0 * l / q -
+                         2.0 * (3.0 * a + 2.0 * l) / (q * q) + l * log(16.0) - 4.0 * l * log(q);
+      return -pi * l / (24.0 * l2 * l2 * log(2.0) * log(2.0)) * pca;
+    }
+    case WL_PROFILE_FIXFLUX: {  // EffAct.c:242-253
+      const double q2 = 0.0742478, q3 = 0.0187671, l = sqrt(l2);
+      const double A = q3 * (a * a / (l2 * q2 * q2)), r = (l - lmin) / (a - lmin);
+      const double ffca = 4.0 * A + r * ((9.0 / 4.0 * A - 9.0 / 2.0) * r - 6.0 * A + 12.0);
+      return -pi * F * F / (e * e * a * a) * ffca;
+    }
+    default: return NAN;
+  }
+}
+
+int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F, int nT,
+                        const double *host_T, int group, int nrho, double *out_action,
+                        double *out_err, double *out_classical, double *out_groups) {
+  if (!ctx) return WL_ERR_INVALID;
+  if (!field || !out_action || !out_err) return fail(ctx, WL_ERR_INVALID, "NULL argument");
+  if (nrho < 1 || nrho > 4096) return fail(ctx, WL_ERR_INVALID, "nrho must be in [1, 4096]");
+  if (!isfinite(F)) return fail(ctx, WL_ERR_INVALID, "F is not finite");
+  const int p = field->profile;
+  if (p == WL_PROFILE_LATTICE)
+    return fail(ctx, WL_ERR_INVALID, "the radial integral needs a cylindrically symmetric profile");
+  const bool cell = (p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX);
+  const bool ref = field->mode == WL_MODE_REFCOMPAT;
+  // nodes and weights of the rho integral (of rho I(rho), Jacobian included)
+  std::vector<double> rho, w;
+  if (cell) {  // integrateRhotoa (EffAct.c:83-138): [0, a/2], n = 2 nrho intervals
+    if (!(field->tubedist > 0.0)) return fail(ctx, WL_ERR_INVALID, "tubedist must be positive");
+    const int n = 2 * nrho;
+    const double h = field->tubedist / (2.0 * n);
+    for (int k = 0; k <= n; ++k) {
+      rho.push_back(h * k);
+      double wk;
+      if (ref) {
+        // the reference adds f(0) + f(a/2) once, then every rho = h(i + 1),
+        // i = 0..n-1, with weight 2 for even i and 4 for odd i -- f(a/2)
+        // twice and the 2/4 weights on the opposite points of Simpson's rule
+        wk = (k == 0) ? 1.0 : (((k - 1) % 2 == 0) ? 2.0 : 4.0);
+        if (k == n) wk += 1.0;
+      } else {
+        wk = (k == 0 || k == n) ? 1.0 : (k % 2 ? 4.0 : 2.0);
+      }
+      w.push_back(wk * h / 3.0);
+    }
+  } else {  // integrateRho (EffAct.c:140-210): rho = (1 - t)/t, t in (0, 1], n panels
+    const int n = nrho;
+    const double h = 1.0 / n;
+    // panel i: t_i = h i, t_{i+1/2}, t_{i+1}; the reference evaluates
+    // f(t_{i+1}) in place of f(t_i) (rhort and rhortp1 are the same point)
+    std::vector<double> wt(2 * n + 1, 0.0);  // weights on t_k = k h/2
+    for (int i = 0; i < n; ++i) {
+      if (ref) {
+        wt[2 * i + 2] += 2.0 * h / 6.0;
+      } else {
+        wt[2 * i] += h / 6.0;
+        wt[2 * i + 2] += h / 6.0;
+      }
+      wt[2 * i + 1] += 4.0 * h / 6.0;
+    }
+    for (int k = 1; k <= 2 * n; ++k) {  // t = 0 (rho = infinity) contributes 0
+      const double t = 0.5 * h * k;
+      rho.push_back((1.0 - t) / t);
+      w.push_back(wt[k] / (t * t));  // d rho = dt / t^2
+    }
+  }
+  const int nr = (int)rho.size();
+  Ensemble e;
+  int r = lookup(ctx, handle, &e);
+  if (r) return r;
+  if (group < 1 || e.Nl % group || e.Nl / group < 2)
+    return fail(ctx, WL_ERR_INVALID, "group %d must divide Nl = %d into at least 2 groups", group,
+                e.Nl);
+  wl::TintArgs ta;
+  if ((r = tint_run(ctx, handle, field, nr, rho.data(), nT, host_T, 1, &F, group, e.Nl / group,
+                    false, &ta)))
+    return r;
+  std::vector<double> Ig((size_t)nr * ta.ng);
+  WL_CHECK(ctx, cudaMemcpyAsync(Ig.data(), ta.Ig, sizeof(double) * Ig.size(),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  if ((r = check_status(ctx))) return r;
+  // Gamma_g = sum_k w_k rho_k I_g(rho_k), normalised as EAction (EffAct.c:289-294)
+  const double norm = field->fermion ? 1.0 / (4.0 * M_PI) : -1.0 / (2.0 * M_PI);
+  std::vector<double> gam(ta.ng, 0.0);
+  for (int k = 0; k < nr; ++k)
+    for (int g = 0; g < ta.ng; ++g) {
+      double v = rho[k] * Ig[(size_t)k * ta.ng + g];
+      if (isinf(v)) v = 0.0;  // EffAct.c:167-181
+      gam[g] += w[k] * v;
+    }
+  double mean = 0.0;
+  for (int g = 0; g < ta.ng; ++g) mean += (gam[g] *= norm);
+  mean /= ta.ng;
+  double ss = 0.0;
+  for (int g = 0; g < ta.ng; ++g) ss += (gam[g] - mean) * (gam[g] - mean);
+  *out_action = mean;
+  *out_err = sqrt(ss / ((double)ta.ng * (ta.ng - 1.0)));
+  if (out_classical)
+    *out_classical = classical_action(p, F, field->lambda2, field->tubedist, field->lmin);
+  if (out_groups) memcpy(out_groups, gam.data(), sizeof(double) * ta.ng);
+  return WL_OK;
 }
 
 int wl_batch_eval(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags) {

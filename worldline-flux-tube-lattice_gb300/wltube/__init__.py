@@ -147,6 +147,8 @@ def lib():
         L.wl_tint.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, C.c_int, dp, C.c_int, dp,
                               C.c_int, C.c_int, dp, dp, dp]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
+        L.wl_effective_action.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_int, dp,
+                                          C.c_int, C.c_int, dp, dp, dp, dp]
         L.wl_batch_eval.argtypes = [vp, C.c_int, C.POINTER(Job), C.c_int]
         L.wl_batch_autotune.argtypes = [vp, C.c_int, C.POINTER(Job), ip, ip]
         L.wl_batch_stats.argtypes = [vp, dp, ip, ip, ip]
@@ -289,6 +291,20 @@ class Context:
                                   nbins, _p(leff, C.c_double), _p(err, C.c_double),
                                   _p(ig, C.c_double) if want_igrand else None))
         return leff, err, ig
+
+    def effective_action(self, handle: int, fld: Field, F: float, T, group: int = 128,
+                         nrho: int = 20):
+        """wl_effective_action: (mean, standard error, classical action,
+        per-group values) of the effective action per unit length."""
+        T = _d(T)
+        Nl = C.c_int()
+        self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), None))
+        groups = np.empty(Nl.value // group)
+        a, e, ca = C.c_double(), C.c_double(), C.c_double()
+        self._check(lib().wl_effective_action(self._h, handle, C.byref(fld), float(F), len(T),
+                                              _p(T, C.c_double), group, nrho, C.byref(a),
+                                              C.byref(e), C.byref(ca), _p(groups, C.c_double)))
+        return a.value, e.value, ca.value, groups
 
     def _jobs(self, jobs):
         """Pack job dicts (handle, field, cx, cy, T, F, group) into wl_job
