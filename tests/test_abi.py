@@ -48,6 +48,14 @@ def test_legacy_symbols_exported(libs):
         assert hasattr(libs["wlhost"], n), n
 
 
+def test_host_file_symbols_exported(libs):
+    names = declared("wl_host.h")
+    assert set(names) == {"wlh_putwl", "wlh_write_ensemble", "wlh_ensemble_file_info",
+                          "wlh_read_ensemble"}
+    for n in names:
+        assert hasattr(libs["wlhost"], n), n
+
+
 def test_version_string_without_gpu(libs):
     f = libs["wlgpu"].wl_version
     f.restype = ctypes.c_char_p

@@ -7,6 +7,8 @@
  *   getwl       text ensemble reader                   (getwl.c:6-40)
  *   Tfunc       proper-time integrand per loop group   (Integrand.c:195-316)
  *   integrateT  Simpson over t in (0,1], T = (1-t)/t   (Tint.c:15-33, 100-175)
+ * and, without counterpart in the reference (wl_host.h), the writer of the
+ * text format and a binary ensemble file format.
  * The field profile is the one EV() uses (wl_legacy_configure / _query).
  * Physical constants follow Integrand.c:11-14 (m^2 = 1, e = 0.30282212).
  *
@@ -17,10 +19,12 @@
  * (T -> infinity) taken as 0.
  */
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#include "../../include/wl_host.h"
 #include "../../include/wl_legacy.h"
 #include "../../include/wlgpu.h"
 
@@ -243,3 +247,97 @@ WLH_API int wlh_putwl(const float4 *worldlines, const char *filename, int Nl, in
     }
   return fclose(fp) == 0 ? 0 : -1;
 }
+
+/* ---- binary ensemble files --------------------------------------------- */
+/* Layout (little-endian): bytes 0-7 the magic "WLENSv1" + NUL, 8-11 Nl,
+ * 12-15 ppl, 16-23 the generator seed (0 if none), 24-27 the values per point
+ * (4: the float4 x, y, z, w), 28-31 zero; then Nl * ppl points of four IEEE-754
+ * binary32 values, loop-major, as the device holds them. */
+static const char wlh_magic[8] = {'W', 'L', 'E', 'N', 'S', 'v', '1', 0};
+
+static void wlh_put32(unsigned char *b, uint32_t v) {
+  for (int i = 0; i < 4; i++) b[i] = (unsigned char)(v >> (8 * i));
+}
+static uint32_t wlh_get32(const unsigned char *b) {
+  uint32_t v = 0;
+  for (int i = 0; i < 4; i++) v |= (uint32_t)b[i] << (8 * i);
+  return v;
+}
+static int wlh_little_endian(void) {
+  const uint32_t one = 1;
+  unsigned char c;
+  memcpy(&c, &one, 1);
+  return c == 1;
+}
+static void wlh_swap_floats(float *v, size_t n) {
+  for (size_t i = 0; i < n; i++) {
+    uint32_t u;
+    memcpy(&u, &v[i], 4);
+    u = (u >> 24) | ((u >> 8) & 0xff00u) | ((u << 8) & 0xff0000u) | (u << 24);
+    memcpy(&v[i], &u, 4);
+  }
+}
+
+WLH_API int wlh_write_ensemble(const char *path, const float4 *loops, int Nl, int ppl,
+                               uint64_t seed) {
+  if (!path || !loops || Nl < 1 || ppl < 1) return -1;
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return -1;
+  unsigned char hdr[32] = {0};
+  memcpy(hdr, wlh_magic, 8);
+  wlh_put32(hdr + 8, (uint32_t)Nl);
+  wlh_put32(hdr + 12, (uint32_t)ppl);
+  wlh_put32(hdr + 16, (uint32_t)seed);
+  wlh_put32(hdr + 20, (uint32_t)(seed >> 32));
+  wlh_put32(hdr + 24, 4u);
+  int ok = fwrite(hdr, 1, 32, fp) == 32;
+  const size_t n = (size_t)Nl * ppl * 4;
+  if (ok && wlh_little_endian()) {
+    ok = fwrite(loops, sizeof(float), n, fp) == n;
+  } else if (ok) {
+    float buf[1024];
+    const float *src = (const float *)loops;
+    for (size_t i = 0; i < n && ok; i += 1024) {
+      const size_t m = n - i < 1024 ? n - i : 1024;
+      memcpy(buf, src + i, m * sizeof(float));
+      wlh_swap_floats(buf, m);
+      ok = fwrite(buf, sizeof(float), m, fp) == m;
+    }
+  }
+  if (fclose(fp) != 0) ok = 0;
+  return ok ? 0 : -1;
+}
+
+/* header of an ensemble file: 0, or -1 (unreadable, not an ensemble file) */
+WLH_API int wlh_ensemble_file_info(const char *path, int *Nl, int *ppl, uint64_t *seed) {
+  if (!path) return -1;
+  FILE *fp = fopen(path, "rb");
+  if (!fp) return -1;
+  unsigned char hdr[32];
+  const int ok = fread(hdr, 1, 32, fp) == 32 && memcmp(hdr, wlh_magic, 8) == 0 &&
+                 wlh_get32(hdr + 24) == 4u;
+  fclose(fp);
+  if (!ok) return -1;
+  const uint32_t nl = wlh_get32(hdr + 8), pp = wlh_get32(hdr + 12);
+  if (nl < 1 || pp < 1 || nl > 0x7fffffffu || pp > 0x7fffffffu) return -1;
+  if (Nl) *Nl = (int)nl;
+  if (ppl) *ppl = (int)pp;
+  if (seed) *seed = (uint64_t)wlh_get32(hdr + 16) | ((uint64_t)wlh_get32(hdr + 20) << 32);
+  return 0;
+}
+
+/* reads the points into loops[Nl * ppl] (sizes from wlh_ensemble_file_info):
+ * 0, or -1 if the file is unreadable, of another shape or short */
+WLH_API int wlh_read_ensemble(const char *path, float4 *loops, int Nl, int ppl) {
+  int fn = 0, fp_ = 0;
+  if (!loops || wlh_ensemble_file_info(path, &fn, &fp_, NULL) || fn != Nl || fp_ != ppl)
+    return -1;
+  FILE *fp = fopen(path, "rb");
+  if (!fp) return -1;
+  const size_t n = (size_t)Nl * ppl * 4;
+  int ok = fseek(fp, 32, SEEK_SET) == 0 && fread(loops, sizeof(float), n, fp) == n;
+  fclose(fp);
+  if (ok && !wlh_little_endian()) wlh_swap_floats((float *)loops, n);
+  return ok ? 0 : -1;
+}
+

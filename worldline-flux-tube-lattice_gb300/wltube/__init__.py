@@ -173,6 +173,43 @@ def lib():
     return _lib
 
 
+_host = None
+
+
+def host_lib():
+    """The loaded libwlhost.so (the C host layer and the ensemble files)."""
+    global _host
+    if _host is None:
+        lib()
+        H = C.CDLL(os.path.join(PKG, "lib", "libwlhost.so"))
+        vp, ip = C.c_void_p, C.POINTER(C.c_int)
+        H.wlh_write_ensemble.argtypes = [C.c_char_p, vp, C.c_int, C.c_int, C.c_uint64]
+        H.wlh_ensemble_file_info.argtypes = [C.c_char_p, ip, ip, C.POINTER(C.c_uint64)]
+        H.wlh_read_ensemble.argtypes = [C.c_char_p, vp, C.c_int, C.c_int]
+        _host = H
+    return _host
+
+
+def save_ensemble(path: str, loops: np.ndarray, seed: int = 0):
+    """Write a [Nl][ppl][4] float32 ensemble as a binary ensemble file."""
+    loops = np.ascontiguousarray(loops, dtype=np.float32)
+    Nl, ppl = loops.shape[:2]
+    if host_lib().wlh_write_ensemble(path.encode(), loops.ctypes.data, Nl, ppl, seed) != 0:
+        raise OSError("cannot write ensemble file %s" % path)
+
+
+def load_ensemble(path: str):
+    """(loops [Nl][ppl][4] float32, seed) of a binary ensemble file."""
+    nl, ppl, seed = C.c_int(), C.c_int(), C.c_uint64()
+    H = host_lib()
+    if H.wlh_ensemble_file_info(path.encode(), C.byref(nl), C.byref(ppl), C.byref(seed)):
+        raise OSError("not an ensemble file: %s" % path)
+    out = np.empty((nl.value, ppl.value, 4), dtype=np.float32)
+    if H.wlh_read_ensemble(path.encode(), out.ctypes.data, nl.value, ppl.value):
+        raise OSError("cannot read ensemble file %s" % path)
+    return out, seed.value
+
+
 def _d(a):
     return np.ascontiguousarray(np.atleast_1d(a), dtype=np.float64)
 
