@@ -43,6 +43,16 @@ extern "C" {
 #define WL_PROFILE_QUADRATIC 2
 #define WL_PROFILE_GAUSSIAN 3
 #define WL_PROFILE_PERIODIC 4
+/* the tabulated profile of periodic.c:17-164: f(rho) integrates
+ * (2/lambda^2) rho exp(-sin^2(pi rho/a)/lambda^2) from 0 on 1000 knots over
+ * rho in (0, 20], interpolated by a clamped cubic spline in rho^2 (0 outside
+ * the table, as interp, intEV.cu:64-107).  f' is the reference kernel's
+ * exp(-sin^2(pi rho)/lambda^2)/lambda^2 (intEV.cu:389-397, which leaves a out)
+ * in WL_MODE_REFCOMPAT and the derivative of the tabulated f (sin(pi rho/a))
+ * in WL_MODE_EXACT.  The reference builds the table with GSL's ODE stepper,
+ * which is not available here: this library integrates with Gauss-Legendre
+ * quadrature per knot interval (the right-hand side does not depend on f). */
+#define WL_PROFILE_SPLINE 5
 #define WL_PROFILE_FIXFLUX 6
 /* Square lattice of identical Gaussian flux tubes at R = a(m, n), |R| <=
  * rimage (no counterpart in the reference, whose "periodic" profile is a
@@ -169,6 +179,12 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
  * (fma.rn.f32x2, two FMAs per instruction).  *ops_per_s receives
  * lane operations per second over the whole device (about 0.1 s of work). */
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s);
+
+/* The spline profile's table for lambda^2 and the tube spacing (host only, no
+ * device needed): knots rho2[n] (rho_i^2 as float, rho_i = 20 i/n) and the
+ * spline coefficients coef4[n][4] = (f, b, c, d) of f + b d + c d^2 + d d^3,
+ * d = rho^2 - rho2[i] (periodic.c:46-164 builds the same table). */
+int wl_spline_table(double lambda2, double tubedist, int n, float *rho2, float *coef4);
 
 /* Allocation-free variant of wl_eval_device.  No counterpart in the
  * reference.  For callers that cannot let a library allocate device memory:

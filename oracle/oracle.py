@@ -97,6 +97,9 @@ def lib():
         L.wlo64_fl_over_rho2.argtypes = [C.c_double, Fp]
         L.wlo64_idt.argtypes = [C.c_double, C.c_double, C.c_double, Fp, dp, dp]
         L.wlo_set_lattice_rcut.argtypes = [C.c_double]
+        L.wlo_spline_table.argtypes = [C.c_double, C.c_double, C.c_int, dp, dp]
+        L.wlo_spline_eval.restype = C.c_double
+        L.wlo_spline_eval.argtypes = [C.c_double, Fp]
         L.wlo64_loop_sums.argtypes = [fp, C.c_int, C.c_double, C.c_double, C.c_double,
                                       Fp, dp, dp]
         L.wlo32_loop_sums.argtypes = [fp, C.c_int, C.c_float, C.c_float, C.c_float,
@@ -155,6 +158,17 @@ def set_lattice_rcut(r_over_lambda: float):
     """Near-image margin of the lattice sum in units of lambda (<= 0: every
     image with |R| <= rimage)."""
     lib().wlo_set_lattice_rcut(C.c_double(r_over_lambda))
+
+
+def spline_table(lambda2, a, n=1000):
+    """The oracle's spline-profile table: knots rho^2 (float values) and f."""
+    x, f = np.empty(n), np.empty(n)
+    lib().wlo_spline_table(lambda2, a, n, _ptr(x, C.c_double), _ptr(f, C.c_double))
+    return x, f
+
+
+def spline_eval(rho2, fld):
+    return lib().wlo_spline_eval(float(rho2), C.byref(fld))
 
 
 def philox(ctr, key):

@@ -20,6 +20,118 @@
 #define WLO_Q1 0.443991  /* fixflux constants (analysis-scripts/EAscffvsconst.sage:6-7) */
 #define WLO_Q2 0.0742478
 
+/* ------------------------------------------------------ spline profile -- */
+/* periodic.c:17-164: f(rho) = int_0^rho (2/lambda^2) s exp(-sin^2(pi s/a)/
+ * lambda^2) ds at the knots rho_i = i h, i = 1..n, h = 20/n (the reference
+ * steps an 8th-order Runge-Kutta; here: composite Simpson with 256
+ * sub-intervals per step), then the clamped cubic spline with zero end slopes
+ * in x = rho^2 at the knots rounded to float (periodic.c:46-110; here in the
+ * second-derivative form, solved by the Thomas algorithm).  interp
+ * (intEV.cu:64-107) gives 0 outside (x_0, x_{n-1}).  One table is kept, for
+ * the last (lambda^2, a).                                                      */
+static struct {
+  double l2, a;
+  int n;
+  double *x, *f, *M;
+} g_sp = {0, 0, 0, NULL, NULL, NULL};
+
+static void spline_build(double l2, double a, int n) {
+  if (g_sp.n == n && g_sp.l2 == l2 && g_sp.a == a) return;
+  free(g_sp.x);
+  free(g_sp.f);
+  free(g_sp.M);
+  g_sp.x = (double *)malloc(sizeof(double) * n);
+  g_sp.f = (double *)malloc(sizeof(double) * n);
+  g_sp.M = (double *)malloc(sizeof(double) * n);
+  const double h = 20.0 / n;
+  const int sub = 256;
+  double acc = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double lo = i * h, dh = h / sub;
+    double s = 0.0;
+    for (int k = 0; k <= sub; k++) {
+      const double t = lo + k * dh, sn = sin(M_PI * t / a);
+      const double v = 2.0 / l2 * t * exp(-sn * sn / l2);
+      s += (k == 0 || k == sub) ? v : (k % 2 ? 4.0 * v : 2.0 * v);
+    }
+    acc += s * dh / 3.0;
+    const double r = (i + 1) * h;
+    g_sp.x[i] = (double)(float)(r * r);
+    g_sp.f[i] = acc;
+  }
+  /* second derivatives M: h_{i-1} M_{i-1} + 2 (h_{i-1} + h_i) M_i + h_i M_{i+1}
+   * = 6 (slope_i - slope_{i-1}), with S'(x_0) = S'(x_{n-1}) = 0 at the ends */
+  double *dg = (double *)malloc(sizeof(double) * n), *up = (double *)malloc(sizeof(double) * n);
+  double *lo = (double *)malloc(sizeof(double) * n), *rhs = (double *)malloc(sizeof(double) * n);
+  for (int i = 0; i < n; i++) {
+    const double hl = i > 0 ? g_sp.x[i] - g_sp.x[i - 1] : 0.0;
+    const double hr = i < n - 1 ? g_sp.x[i + 1] - g_sp.x[i] : 0.0;
+    const double sl = i > 0 ? (g_sp.f[i] - g_sp.f[i - 1]) / hl : 0.0;
+    const double sr = i < n - 1 ? (g_sp.f[i + 1] - g_sp.f[i]) / hr : 0.0;
+    lo[i] = hl;
+    dg[i] = 2.0 * (hl + hr);
+    up[i] = hr;
+    rhs[i] = 6.0 * (sr - sl);
+  }
+  for (int i = 1; i < n; i++) { /* forward elimination */
+    const double m = lo[i] / dg[i - 1];
+    dg[i] -= m * up[i - 1];
+    rhs[i] -= m * rhs[i - 1];
+  }
+  g_sp.M[n - 1] = rhs[n - 1] / dg[n - 1];
+  for (int i = n - 2; i >= 0; i--) g_sp.M[i] = (rhs[i] - up[i] * g_sp.M[i + 1]) / dg[i];
+  free(dg);
+  free(up);
+  free(lo);
+  free(rhs);
+  g_sp.l2 = l2;
+  g_sp.a = a;
+  g_sp.n = n;
+}
+
+/* builds the table before any parallel region reads it */
+static void spline_prepare(const wlo_field *fl) {
+  if (fl->profile == WLO_SPLINE) spline_build(fl->lambda2, fl->tubedist, 1000);
+}
+
+static double spline_f(double r2, const wlo_field *fl) {
+  /* parallel callers prepared the table; single-threaded ones may build here */
+  if (g_sp.n != 1000 || g_sp.l2 != fl->lambda2 || g_sp.a != fl->tubedist)
+    spline_build(fl->lambda2, fl->tubedist, 1000);
+  const int n = g_sp.n;
+  const double *x = g_sp.x;
+  if (!(r2 < x[n - 1] && r2 > x[0])) return 0.0;
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (r2 >= x[mid]) lo = mid;
+    else hi = mid;
+  }
+  const double h = x[hi] - x[lo], A = (x[hi] - r2) / h, B = (r2 - x[lo]) / h;
+  return A * g_sp.f[lo] + B * g_sp.f[hi] +
+         ((A * A * A - A) * g_sp.M[lo] + (B * B * B - B) * g_sp.M[hi]) * h * h / 6.0;
+}
+
+/* f' of the spline profile: the reference kernel's sin(pi sqrt(rho2))
+ * (intEV.cu:389-397, no tube spacing) in ref-compat mode, the derivative of
+ * the tabulated f, sin(pi sqrt(rho2)/a), in exact mode */
+static double spline_fp(double r2, const wlo_field *fl) {
+  const double arg = fl->mode == WLO_EXACT ? M_PI / fl->tubedist : M_PI;
+  const double s = sin(sqrt(r2) * arg);
+  return exp(-s * s / fl->lambda2) / fl->lambda2;
+}
+
+void wlo_spline_table(double lambda2, double a, int n, double *x, double *f) {
+  spline_build(lambda2, a, n);
+  memcpy(x, g_sp.x, sizeof(double) * n);
+  memcpy(f, g_sp.f, sizeof(double) * n);
+}
+
+double wlo_spline_eval(double r2, const wlo_field *fl) {
+  spline_prepare(fl);
+  return spline_f(r2, fl);
+}
+
 /* ---------------------------------------------------------------- FP64 -- */
 #define REAL double
 #define SFX(name) d_##name
@@ -65,9 +177,15 @@
 #include "wl_oracle_body.h"
 
 /* ------------------------------------------------------------ exports -- */
-double wlo64_flambda(double rho2, const wlo_field *f) { return d_flambda(rho2, f); }
+double wlo64_flambda(double rho2, const wlo_field *f) {
+  spline_prepare(f);
+  return d_flambda(rho2, f);
+}
 double wlo64_fplambda(double rho2, const wlo_field *f) { return d_fplambda(rho2, f); }
-double wlo64_fl_over_rho2(double rho2, const wlo_field *f) { return d_flrho2(rho2, f); }
+double wlo64_fl_over_rho2(double rho2, const wlo_field *f) {
+  spline_prepare(f);
+  return d_flrho2(rho2, f);
+}
 
 void wlo64_idt(double a, double b, double c, const wlo_field *f, double *scalI,
                double *fermI) {
@@ -142,6 +260,7 @@ static void finish_loop(const double gs[3], const double gf[3], double T, double
 void wlo64_loops(const float *loops, int Nl, int ppl, double cx, double cy, double T,
                  double F, const wlo_field *f, double *scal, double *ferm) {
   const double rtT = sqrt(T);
+  spline_prepare(f);
 #pragma omp parallel for schedule(dynamic, 4)
   for (int l = 0; l < Nl; l++) {
     double gs[3], gf[3];
@@ -203,6 +322,7 @@ static void eval_generic(int fp32, const float *loops, int Nl, int ppl, int nins
 #else
   (void)nthreads;
 #endif
+  spline_prepare(f);
   /* one task per (instance, group); loops of a group are summed in order */
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
   for (long task = 0; task < (long)ninst * ng; task++) {
@@ -306,6 +426,11 @@ double wlo_magfield(double rho2, double F, const wlo_field *f, const wlo_qed *q)
     case WLO_QUADRATIC: B = rho2 < l2 ? 2.0 / l2 * (1.0 - rho2 / l2) : 0.0; break;
     case WLO_GAUSSIAN: B = rho2 < 100.0 * l2 ? 1.0 / (l2 * exp(rho2 / l2)) : 0.0; break;
     case WLO_PERIODIC: B = d_periodicB(rho2, f); break;
+    case WLO_SPLINE: {  /* Integrand.c:128-131 */
+      const double sr = sin(M_PI * sqrt(rho2) / f->tubedist);
+      B = 1.0 / (l2 * exp(sr * sr / l2));
+      break;
+    }
     case WLO_FIXFLUX: B = d_fixfluxB(rho2, f); break;
     case WLO_LATTICE: {
       /* no reference: the images' Gaussian fields at (sqrt(rho2), 0) */
@@ -361,6 +486,11 @@ int wlo_tfunc_regime(double T, double xcmx, double xcmy, double F, const wlo_fie
     case WLO_PERIODIC: smallT = 0.5 * (l2 + rho * rho); break;
     case WLO_GAUSSIAN:
     case WLO_LATTICE: smallT = l2; break;
+    case WLO_SPLINE: {  /* Integrand.c:209, 236-240 */
+      const double a = f->tubedist, s2 = sin(2.0 * M_PI * rho / a);
+      smallT = rho / a > 1.0e-8 ? a * a * l2 / (M_PI * M_PI * s2 * s2) : 1.0e12;
+      break;
+    }
     case WLO_FIXFLUX:
       smallT = rho * rho < l2 / 4.0 ? 0.25 * l2
                                     : 0.25 * l2 + (rho - sqrt(l2) / 2.0) * (rho - sqrt(l2) / 2.0);
@@ -415,6 +545,7 @@ void wlo64_integrateT(const float *loops, int Nl, int ppl, int n, int ng, double
                       double xcmy, double F, const wlo_field *f, const wlo_qed *q,
                       double *val, double *leff, double *sem, int nthreads) {
   (void)Nl;
+  spline_prepare(f);
   const double h = 1.0 / (double)n;
   double *trt = (double *)malloc(sizeof(double) * ng);
   double *trh = (double *)malloc(sizeof(double) * ng);

@@ -64,6 +64,11 @@ typedef struct {
  * wlo_set_lattice_rcut(r) sets rcut / lambda (r <= 0: sum every image with
  * |R| <= rimage), which the tests use to check the selection.              */
 #define WLO_LATTICE_RCUT_L 4.242640687119285 /* sqrt(18) */
+
+/* the spline profile's table (knots x = rho^2 as float values, f at the
+ * knots) for lambda^2 and a with n knots, and its interpolant at rho2 */
+void wlo_spline_table(double lambda2, double a, int n, double *x, double *f);
+double wlo_spline_eval(double rho2, const wlo_field *f);
 void wlo_set_lattice_rcut(double r_over_lambda);
 
 /* ---- profiles (FP64) -------------------------------------------------- */

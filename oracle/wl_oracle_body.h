@@ -142,6 +142,7 @@ static REAL SFX(flambda)(REAL r2, const wlo_field *f) {
     case WLO_QUADRATIC: return r2 < l2 ? r2 / l2 * ((REAL)2 - r2 / l2) : (REAL)1;
     case WLO_GAUSSIAN: return GAUSS_1MEXP(r2 / l2);
     case WLO_PERIODIC: return SFX(flperi)(r2, l2, (REAL)f->tubedist);
+    case WLO_SPLINE: return (REAL)spline_f((double)r2, f);
     case WLO_FIXFLUX:
       return SFX(ffixflux)(r2, l2, (REAL)f->tubedist, (REAL)f->lmin, f->ff_variant);
     default: return (REAL)0;
@@ -172,6 +173,7 @@ static REAL SFX(fplambda)(REAL r2, const wlo_field *f) {
     case WLO_QUADRATIC: return r2 < l2 ? (REAL)2 / l2 * ((REAL)1 - r2 / l2) : (REAL)0;
     case WLO_GAUSSIAN: return (REAL)1 / l2 * EXP(-r2 / l2);
     case WLO_PERIODIC: return SFX(fplperi)(r2, l2, (REAL)f->tubedist);
+    case WLO_SPLINE: return (REAL)spline_fp((double)r2, f);
     case WLO_FIXFLUX:
       return SFX(fpfixflux)(r2, l2, (REAL)f->tubedist, (REAL)f->lmin);
     default: return (REAL)0;

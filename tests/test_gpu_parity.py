@@ -286,3 +286,26 @@ def test_lattice_matches_oracle(ctx, wl, a, l2, fe):
     assert np.all(err[:, 0, :] <= W_TOL * (1.0 + psi[:, None] / 25.0))
     os_, of = O.loops_phases(loops, cx[5], cy[5], T[5], 1.0, ofld)
     assert np.abs(s[:, :3] - os_).max() / np.abs(os_).max() < PHASE_TOL
+
+
+@pytest.mark.parametrize("mode,fe,a", [(0, 0, 1.0), (0, 1, 1.0), (1, 1, 2.0), (1, 0, 2.0)])
+def test_spline_profile_matches_oracle(ctx, wl, mode, fe, a):
+    """The tabulated profile of periodic.c (the library's table against the
+    oracle's independently built one), per-loop phases and <W> per group."""
+    loops = O.vloops(6, 256, 256)
+    cx, cy, T = _instances(96, 2.0 * a, 0.01, 4.0, 13)
+    F = [0.5, 1.0]
+    fld = wl.field("spline", fermion=fe, nint=8, mode=mode, lambda2=0.5, tubedist=a)
+    ofld = O.field("spline", fermion=fe, nint=8, mode=mode, lambda2=0.5, tubedist=a)
+    h = ctx.upload(loops)
+    try:
+        g, _, _ = ctx.eval(h, fld, cx, cy, T, F)
+        s, f = ctx.loops(h, fld, float(cx[5]), float(cy[5]), float(T[5]), 1.0)
+    finally:
+        ctx.release(h)
+    ref, S = O.eval_groups(loops, cx, cy, T, F, ofld, return_scale=True)
+    assert werr(g, ref, S) < W_TOL
+    rs, rf = O.loops_phases(loops, float(cx[5]), float(cy[5]), float(T[5]), 1.0, ofld)
+    assert np.abs(s[:, :3] - rs).max() / max(np.abs(rs).max(), 1e-30) < PHASE_TOL
+    if fe:
+        assert np.abs(f[:, :3] - rf).max() / max(np.abs(rf).max(), 1e-30) < PHASE_TOL

@@ -27,7 +27,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 SOURCES = ["wl_sweep_smooth.cu", "wl_sweep_simple.cu", "wl_sweep_periodic.cu",
            "wl_sweep_lattice.cu",
            "wl_sweep_fixflux.cu", "wl_misc.cu", "wl_api.cpp", "wl_noalloc.cu",
-           "wl_tint.cu", "wl_batch.cu", "wl_server.cpp"]
+           "wl_tint.cu", "wl_batch.cu", "wl_server.cpp", "wl_spline.cpp"]
 
 
 def nvcc() -> str:

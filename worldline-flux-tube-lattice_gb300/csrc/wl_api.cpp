@@ -19,6 +19,7 @@
 #include "../../include/wl_legacy.h"
 #include "../../include/wlgpu.h"
 #include "wl_internal.h"
+#include "wl_spline.h"
 
 using wl::FieldDev;
 
@@ -84,6 +85,8 @@ struct wl_ctx {
   int last_launches = 0;
   const char *last_kind = "none";
   AddressRangeFn addr_range = nullptr;
+  // spline profile tables on the device, by (lambda^2, a)
+  std::map<std::pair<double, double>, std::pair<float *, float4 *>> splines;
 };
 
 namespace {
@@ -140,7 +143,7 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
   int p = f->profile;
   if (!(p == WL_PROFILE_STEP || p == WL_PROFILE_SMOOTH || p == WL_PROFILE_QUADRATIC ||
         p == WL_PROFILE_GAUSSIAN || p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX ||
-        p == WL_PROFILE_LATTICE))
+        p == WL_PROFILE_LATTICE || p == WL_PROFILE_SPLINE))
     return fail(ctx, WL_ERR_INVALID, "unsupported profile %d", p);
   if (p == WL_PROFILE_LATTICE) {
     if (f->mode != WL_MODE_EXACT)
@@ -155,13 +158,14 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
     return fail(ctx, WL_ERR_INVALID, "unknown mode %d", f->mode);
   if (!(f->lambda2 > 0.0) || !isfinite(f->lambda2))
     return fail(ctx, WL_ERR_INVALID, "lambda2 must be positive");
-  if ((p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX) &&
+  if ((p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX || p == WL_PROFILE_SPLINE) &&
       (!(f->tubedist > 0.0) || !isfinite(f->tubedist)))
     return fail(ctx, WL_ERR_INVALID, "tubedist must be positive");
   if (p == WL_PROFILE_FIXFLUX && !(f->tubedist > f->lmin))
     return fail(ctx, WL_ERR_INVALID, "fixflux needs tubedist > lmin");
   *kprofile = (p == WL_PROFILE_FIXFLUX && f->ff_variant) ? wl::kFixfluxFF : p;
   if (p == WL_PROFILE_LATTICE) *kprofile = wl::kLattice;
+  if (p == WL_PROFILE_SPLINE) *kprofile = wl::kSpline;
   memset(d, 0, sizeof(*d));
   d->l2 = (float)f->lambda2;
   d->inv_l2 = 1.0f / d->l2;
@@ -179,11 +183,19 @@ int field_to_dev(wl_ctx *ctx, const wl_field *f, int *kprofile, FieldDev *d) {
     d->rimg2 = (float)(rr * rr * (1.0 + 1e-6));
     d->rcut = (float)(4.242640687119285 * sqrt(f->lambda2));  // sqrt(18) lambda
   }
+  if (p == WL_PROFILE_SPLINE) {  // the table itself is attached per context
+    d->sp_n = wl::kSplineKnots;
+    d->sp_h = (float)(20.0 / wl::kSplineKnots);
+    // f' argument: the reference kernel's sin(pi rho) (intEV.cu:391) or the
+    // derivative of the tabulated profile, sin(pi rho / a)
+    d->sp_piarg = (float)(f->mode == WL_MODE_REFCOMPAT ? M_PI : M_PI / f->tubedist);
+  }
   if (f->mode == WL_MODE_REFCOMPAT) {
     d->clampA = d->clampB = d->clampC = d->clampE = 1.0e-8f;
     d->clampI = 1.0e-10f;
   } else {
-    const bool divides = (p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX);
+    const bool divides =
+        (p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX || p == WL_PROFILE_SPLINE);
     const float fl = divides ? 1.0e-30f : -INFINITY;
     d->clampA = d->clampE = d->clampI = fl;
     d->clampB = d->clampC = -INFINITY;
@@ -244,6 +256,32 @@ int ensure_bbox(wl_ctx *ctx, int handle, const float4 **out) {
     WL_CHECK(ctx, wl::launch_loop_bbox(e.dev, e.Nl, e.ppl, e.bbox, ctx->stream));
   }
   *out = e.bbox;
+  return WL_OK;
+}
+
+// the spline profile's table for (lambda^2, a) on the device, built once
+int ensure_spline(wl_ctx *ctx, const wl_field *f, FieldDev *d) {
+  const auto key = std::make_pair(f->lambda2, f->tubedist);
+  auto it = ctx->splines.find(key);
+  if (it == ctx->splines.end()) {
+    const int n = wl::kSplineKnots;
+    std::vector<float> rho2(n), coef(4 * (size_t)n);
+    if (wl::spline_table(f->lambda2, f->tubedist, n, rho2.data(), coef.data()))
+      return fail(ctx, WL_ERR_INVALID, "spline table: invalid lambda2 or tubedist");
+    float *dr = nullptr;
+    float4 *dc = nullptr;
+    if (cudaMalloc((void **)&dr, sizeof(float) * n) != cudaSuccess ||
+        cudaMalloc((void **)&dc, sizeof(float4) * n) != cudaSuccess) {
+      cudaGetLastError();
+      if (dr) cudaFree(dr);
+      return fail(ctx, WL_ERR_NOMEM, "cannot allocate the spline table");
+    }
+    WL_CHECK(ctx, cudaMemcpy(dr, rho2.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    WL_CHECK(ctx, cudaMemcpy(dc, coef.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    it = ctx->splines.emplace(key, std::make_pair(dr, dc)).first;
+  }
+  d->sp_rho2 = it->second.first;
+  d->sp_coef = it->second.second;
   return WL_OK;
 }
 
@@ -640,6 +678,11 @@ int wl_ctx_destroy(wl_ctx *ctx) {
   ctx->out.release();
   ctx->status.release();
   ctx->list.release();
+  for (auto &kv : ctx->splines) {
+    cudaFree(kv.second.first);
+    cudaFree(kv.second.second);
+  }
+  ctx->splines.clear();
   ctx->perm.release();
   ctx->b_perm.release();
   ctx->aux.release();
@@ -793,6 +836,7 @@ static int eval_prologue(wl_ctx *ctx, int handle, const wl_field *field, int nin
   if (group < 1 || e->Nl % group != 0)
     return fail(ctx, WL_ERR_INVALID, "group %d must divide Nl = %d", group, e->Nl);
   if ((r = field_to_dev(ctx, field, kprof, fd))) return r;
+  if (*kprof == wl::kSpline && (r = ensure_spline(ctx, field, fd))) return r;
   for (int j = 0; j < nF; ++j)
     if (!isfinite(host_F[j])) return fail(ctx, WL_ERR_INVALID, "F[%d] is not finite", j);
   return set_device(ctx);
@@ -807,6 +851,8 @@ static int run_eval(wl_ctx *ctx, const Ensemble &e, int kprof, const FieldDev &f
   const bool fermion = field->fermion != 0;
   const int nint = field->nint;
   const bool use_sweep = ninst >= 32;
+  if (kprof == wl::kSpline && (!fd.sp_rho2 || !fd.sp_coef))
+    return fail(ctx, WL_ERR_INVALID, "spline profile without its table");
   int n_chunks, cpg;
   if (use_sweep) {
     const int lc = plan_chunk(group);
@@ -950,6 +996,12 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
     return r;
   ctx->last_launches = 3;
   return WL_OK;
+}
+
+int wl_spline_table(double lambda2, double tubedist, int n, float *rho2, float *coef4) {
+  if (!(lambda2 > 0.0) || !(tubedist > 0.0) || n < 4 || n > (1 << 20) || !rho2 || !coef4)
+    return WL_ERR_INVALID;
+  return wl::spline_table(lambda2, tubedist, n, rho2, coef4) ? WL_ERR_INVALID : WL_OK;
 }
 
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s) {
@@ -1131,6 +1183,7 @@ static double classical_action(int profile, double F, double l2, double a, doubl
                          2.0 * (3.0 * a + 2.0 * l) / (q * q) + l * log(16.0) - 4.0 * l * log(q);
       return -pi * l / (24.0 * l2 * l2 * log(2.0) * log(2.0)) * pca;
     }
+    case WL_PROFILE_SPLINE: return 1.0;  // EffAct.c:272-273 (no closed form there)
     case WL_PROFILE_FIXFLUX: {  // EffAct.c:242-253
       const double q2 = 0.0742478, q3 = 0.0187671, l = sqrt(l2);
       const double A = q3 * (a * a / (l2 * q2 * q2)), r = (l - lmin) / (a - lmin);
@@ -1151,7 +1204,7 @@ int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F
   const int p = field->profile;
   if (p == WL_PROFILE_LATTICE)
     return fail(ctx, WL_ERR_INVALID, "the radial integral needs a cylindrically symmetric profile");
-  const bool cell = (p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX);
+  const bool cell = (p == WL_PROFILE_PERIODIC || p == WL_PROFILE_FIXFLUX || p == WL_PROFILE_SPLINE);
   const bool ref = field->mode == WL_MODE_REFCOMPAT;
   // nodes and weights of the rho integral (of rho I(rho), Jacobian included)
   std::vector<double> rho, w;
@@ -1358,6 +1411,7 @@ int wl_loops(wl_ctx *ctx, int handle, const wl_field *field, double cx, double c
   int kprof;
   FieldDev fd;
   if ((r = field_to_dev(ctx, field, &kprof, &fd))) return r;
+  if (kprof == wl::kSpline && (r = ensure_spline(ctx, field, &fd))) return r;
   if (!isfinite(F)) return fail(ctx, WL_ERR_INVALID, "F is not finite");
   if ((r = set_device(ctx))) return r;
   if ((r = upload_instances(ctx, 1, &cx, &cy, &T, e.ppl))) return r;
@@ -1475,6 +1529,7 @@ double EV(double T, void *p, int *WLlist) {
   int kprof;
   FieldDev fd;
   if (field_to_dev(ctx, &f, &kprof, &fd)) return legacy_fail(ctx->err.c_str());
+  if (kprof == wl::kSpline && ensure_spline(ctx, &f, &fd)) return legacy_fail(ctx->err.c_str());
   const bool hit = L.valid && L.T == T && L.F == params.F && L.l2 == params.l2 &&
                    L.cx == params.xcm.x && L.cy == params.xcm.y &&
                    L.loops == params.worldlines && L.Nl == params.Nl && L.ppl == params.Nppl &&
@@ -1552,8 +1607,10 @@ static void log_simpson_weights(const double *T, int n, double du, double *w);
 // same field validation, flux constants and loop partition as wl_eval_device.
 namespace wl {
 int shared_field_to_dev(const wl_field *f, int *kprofile, FieldDev *d) {
-  // the lattice needs per-loop bounding boxes the library would allocate
-  if (f && f->profile == WL_PROFILE_LATTICE) return WL_ERR_INVALID;
+  // the lattice needs per-loop bounding boxes and the spline profile its
+  // table, both of which the library would allocate
+  if (f && (f->profile == WL_PROFILE_LATTICE || f->profile == WL_PROFILE_SPLINE))
+    return WL_ERR_INVALID;
   return field_to_dev(nullptr, f, kprofile, d);
 }
 void shared_fill_flux(SweepArgs &a, const wl_field *f, int nF, const double *F) {

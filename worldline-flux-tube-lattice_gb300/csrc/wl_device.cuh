@@ -194,6 +194,30 @@ struct Profile<kPeriodic> {  // radial shells, intEV.cu:201-232 and 300-328
   static constexpr bool kHeavy = true;
 };
 
+template <>
+struct Profile<kSpline> {  // interp (intEV.cu:64-107), fplambda spline (intEV.cu:389-397)
+  static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,
+                                              float &fp) {
+    // the interval [rho2[j], rho2[j+1]) of the table; 0 outside, as interp;
+    // the knots are near ((j + 1) h)^2, so the guess is within one knot
+    float f = 0.0f;
+    const int n = F.sp_n;
+    if (F.sp_rho2 && n >= 2 && r2 < F.sp_rho2[n - 1] && r2 > F.sp_rho2[0]) {
+      int j = min(max((int)(sqrtf(r2) / F.sp_h) - 1, 0), n - 2);
+      while (j > 0 && r2 < F.sp_rho2[j]) --j;
+      while (j < n - 2 && r2 >= F.sp_rho2[j + 1]) ++j;
+      const float d = r2 - F.sp_rho2[j];
+      const float4 c = F.sp_coef[j];
+      f = c.x + d * (c.y + d * (c.z + d * c.w));
+    }
+    g = f / r2;
+    const float s = sinf(sqrtf(r2) * F.sp_piarg);
+    fp = expf(-s * s * F.inv_l2) * F.inv_l2;
+  }
+  static __device__ __forceinline__ float fp_scale(const FieldDev &) { return 1.0f; }
+  static constexpr bool kHeavy = true;
+};
+
 template <bool FF>
 struct FixfluxProfile {  // intEV.cu:236-257, 333-357; intEVff.cu:194-250
   static __device__ __forceinline__ void eval(float r2, const FieldDev &F, float &g,

@@ -25,7 +25,8 @@ static cudaError_t dispatch(int profile, bool fermion, int nint, const SweepArgs
     case kStep:
     case kQuadratic:
     case kGaussian: return launch_sweep_simple(profile, fermion, nint, sa, la, s);
-    case kPeriodic: return launch_sweep_periodic(profile, fermion, nint, sa, la, s);
+    case kPeriodic:
+    case kSpline: return launch_sweep_periodic(profile, fermion, nint, sa, la, s);
     case kFixflux:
     case kFixfluxFF: return launch_sweep_fixflux(profile, fermion, nint, sa, la, s);
     case kLattice: return launch_sweep_lattice(profile, fermion, nint, sa, la, s);

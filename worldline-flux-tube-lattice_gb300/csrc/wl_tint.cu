@@ -46,6 +46,11 @@ __device__ double magfield_d(const TintArgs &A, double rho2, double F) {
       B = a / (2.0 * log(2.0) * l2) * f;
       break;
     }
+    case kSpline: {  // Integrand.c:128-131
+      const double s = sin(M_PI * sqrt(rho2) / a);
+      B = 1.0 / (l2 * exp(s * s / l2));
+      break;
+    }
     case kFixflux:
     case kFixfluxFF: {  // Integrand.c:39-56 (the width ratio is a float there)
       const float lf = (float)sqrt(l2), af = (float)a, lmf = (float)A.lmin;
@@ -83,6 +88,11 @@ __device__ double igrand_d(TintArgs A, double rho, double T, double F, double W)
     case kStep: smallT = (double)abs((int)(rho * rho - l2)); break;
     case kGaussian:
     case kLattice: smallT = l2; break;
+    case kSpline: {  // Integrand.c:209, 236-240
+      const double s2 = sin(2.0 * M_PI * rho / A.a);
+      smallT = rho / A.a > 1.0e-8 ? A.a * A.a * l2 / (M_PI * M_PI * s2 * s2) : 1.0e12;
+      break;
+    }
     case kFixflux:
     case kFixfluxFF:
       smallT = rho2 < l2 / 4.0 ? 0.25 * l2 : 0.25 * l2 + (rho - sqrt(l2) / 2.0) * (rho - sqrt(l2) / 2.0);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <vector_types.h>
 
 namespace wl {
 
@@ -11,6 +12,7 @@ enum : int {
   kQuadratic = 2,
   kGaussian = 3,
   kPeriodic = 4,
+  kSpline = 5,     // tabulated profile of periodic.c (clamped cubic spline)
   kFixflux = 6,
   kFixfluxFF = 7,  // fixflux with the intEVff.cu phi/chi fits
   kLattice = 8     // square lattice of Gaussian tubes (image sum)
@@ -32,6 +34,12 @@ struct FieldDev {
   // margin rcut = sqrt(18) lambda around the loop's bounding box (beyond it
   // 1 - e^{-rho^2/lambda^2} rounds to 1 in FP32: the image is pure gauge)
   float rimg2, rcut;
+  // spline: knots (rho^2) and cubic coefficients in device memory, the knot
+  // spacing in rho, and the argument factor of f' (pi, or pi/a in exact mode)
+  const float *sp_rho2;
+  const float4 *sp_coef;
+  int sp_n;
+  float sp_h, sp_piarg;
 };
 
 }  // namespace wl

@@ -71,6 +71,11 @@ static double wlh_magfield(double rho2, double F, double l2, const wlh_cfg *c) {
       B = a / (2.0 * log(2.0) * l2) * f;
       break;
     }
+    case WL_PROFILE_SPLINE: { /* Integrand.c:128-131 */
+      const double s = sin(wlh_pi * sqrt(rho2) / c->a);
+      B = 1.0 / (l2 * exp(s * s / l2));
+      break;
+    }
     case WL_PROFILE_FIXFLUX: {
       /* Integrand.c:39-56: the width ratio is a float there */
       float lf = (float)sqrt(l2), af = (float)a, lmf = (float)c->lmin;
@@ -120,6 +125,11 @@ WLH_API double *Tfunc(double T, void *p, int *order) {
   switch (c.profile) { /* Integrand.c:219-248 */
     case WL_PROFILE_STEP: smallT = (double)abs((int)(rho * rho - l2)); break;
     case WL_PROFILE_GAUSSIAN: smallT = l2; break;
+    case WL_PROFILE_SPLINE: { /* Integrand.c:209, 236-240 */
+      const double s2 = sin(2.0 * wlh_pi * rho / c.a);
+      smallT = rho / c.a > 1.0e-8 ? c.a * c.a * l2 / (wlh_pi * wlh_pi * s2 * s2) : 1.0e12;
+      break;
+    }
     case WL_PROFILE_FIXFLUX:
       smallT = rho * rho < l2 / 4.0 ? 0.25 * l2
                                     : 0.25 * l2 + (rho - sqrt(l2) / 2.0) * (rho - sqrt(l2) / 2.0);

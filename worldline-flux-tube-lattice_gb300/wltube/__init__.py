@@ -18,7 +18,7 @@ PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "lib", "libwlgpu.so")
 
 PROFILES = {"step": 0, "smooth": 1, "quadratic": 2, "gaussian": 3, "periodic": 4,
-            "fixflux": 6, "lattice": 8}
+            "spline": 5, "fixflux": 6, "lattice": 8}
 MODE_REFCOMPAT, MODE_EXACT = 0, 1
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
           -4: "device wait timed out", -5: "unknown handle", -6: "admission rejected"}
@@ -147,6 +147,7 @@ def lib():
         L.wl_tint.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, C.c_int, dp, C.c_int, dp,
                               C.c_int, C.c_int, dp, dp, dp]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
+        L.wl_spline_table.argtypes = [C.c_double, C.c_double, C.c_int, fp, fp]
         L.wl_effective_action.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_int, dp,
                                           C.c_int, C.c_int, dp, dp, dp, dp]
         L.wl_batch_eval.argtypes = [vp, C.c_int, C.POINTER(Job), C.c_int]
@@ -539,6 +540,17 @@ class Server:
         s = ServerStats()
         lib().wl_server_get_stats(self._h, C.byref(s))
         return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+
+def spline_table(lambda2: float, tubedist: float, n: int = 1000):
+    """The spline profile's table: knots rho^2 [n] and coefficients [n][4]."""
+    rho2 = np.empty(n, dtype=np.float32)
+    coef = np.empty((n, 4), dtype=np.float32)
+    st = lib().wl_spline_table(float(lambda2), float(tubedist), int(n), _p(rho2, C.c_float),
+                               _p(coef, C.c_float))
+    if st != 0:
+        raise WlError(st, "wl_spline_table")
+    return rho2, coef
 
 
 def eval_noalloc(dev_loops: int, Nl: int, ppl: int, fld: Field, ninst: int, dev_cx: int,
