@@ -472,13 +472,19 @@ __device__ __noinline__ float2 segment_lattice(float zix, float ziy, float zjx, 
   const float cs = fmaf(dx, dx, dy * dy) * il2;
   const int nint = NINT > 0 ? NINT : F.nint;
   const float h = NINT > 0 ? 1.0f / (float)NINT : F.h;
+  // the whole range inside the disk m^2 + n^2 <= (rimage/a)^2 (the usual
+  // case): no per-row trimming
+  const int mx = max(abs(img.m0), abs(img.m1)), nx = max(abs(img.n0), abs(img.n1));
+  const bool inside = (float)(mx * mx) + (float)(nx * nx) <= F.rimg2;
   for (int m = img.m0; m <= img.m1; ++m) {
     const float ux = fmaf(-(float)m, F.a, zix);
     const float mm = (float)(m * m);
-    // this row's images inside the disk m^2 + n^2 <= (rimage/a)^2 (an interval)
+    // this row's images inside the disk (an interval)
     int lo = img.n0, hi = img.n1;
-    while (lo <= hi && mm + (float)(lo * lo) > F.rimg2) ++lo;
-    while (hi >= lo && mm + (float)(hi * hi) > F.rimg2) --hi;
+    if (!inside) {
+      while (lo <= hi && mm + (float)(lo * lo) > F.rimg2) ++lo;
+      while (hi >= lo && mm + (float)(hi * hi) > F.rimg2) --hi;
+    }
     int n = lo;
     if constexpr (NINT > 0) {
       // two images per step as packed pairs: every FP32 operation of the two
