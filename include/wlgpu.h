@@ -145,21 +145,29 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
             int nT, const double *host_T, int nF, const double *host_F, int group, int nbins,
             double *out_leff, double *out_err, double *out_igrand);
 
+/* proper-time rules of wl_effective_action */
+#define WL_TRULE_LOG 0   /* host_T: a log-spaced grid of nT points, Simpson in ln T
+                            (as wl_tint)                                          */
+#define WL_TRULE_SUBST 1 /* integrateT's rule (Tint.c:100-175): T = (1 - t)/t, nT
+                            Simpson panels in t (rhogrand uses 40, EffAct.c:22);
+                            host_T is ignored                                    */
+
 /* The effective action per unit length (EffAct.c:83-306): the radial
- * integral of rho I_g(rho) with I_g the proper-time integral of wl_tint (flux
- * F, log-spaced T grid), per group g, divided by 4 pi (spinor) or -2 pi
- * (scalar).  Isolated profiles integrate rho over [0, inf) through
- * rho = (1 - t)/t with nrho Simpson panels in t (EffAct.c:140-210); periodic
- * and fixflux over [0, a/2] with 2 nrho intervals (EffAct.c:83-138).  In
- * WL_MODE_REFCOMPAT the two rules keep the reference's weights (each t panel
- * evaluates its right end twice; on [0, a/2] the end a/2 is counted twice
- * and the weights 2 and 4 sit on the opposite points of Simpson's rule); in
- * WL_MODE_EXACT they are Simpson's rule.  Outputs the mean over groups and
+ * integral of rho I_g(rho), I_g the proper-time integral of group g (flux F,
+ * rule t_rule), divided by 4 pi (spinor) or -2 pi (scalar).  Isolated
+ * profiles integrate rho over [0, inf) through rho = (1 - t)/t with nrho
+ * Simpson panels in t (EffAct.c:140-210); periodic, spline and fixflux over
+ * [0, a/2] with 2 nrho intervals (EffAct.c:83-138).  In WL_MODE_REFCOMPAT the
+ * [0, a/2] rule keeps the reference's weights (the end a/2 counted twice,
+ * the weights 2 and 4 on the opposite points of Simpson's rule); in
+ * WL_MODE_EXACT it is Simpson's rule.  (The reference's t-panel rules, which
+ * evaluate each panel's right end twice, equal Simpson's rule here: the
+ * panel ends t = 0 and t = 1 contribute 0.)  Outputs the mean over groups and
  * its standard error, optionally the profile's classical action
  * (EffAct.c:228-279; NaN for the lattice) and the per-group values [Nl/group].
  * No counterpart as one call in the reference, which runs it as its main(). */
-int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F, int nT,
-                        const double *host_T, int group, int nrho, double *out_action,
+int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F, int t_rule,
+                        int nT, const double *host_T, int group, int nrho, double *out_action,
                         double *out_err, double *out_classical, double *out_groups);
 
 /* Asynchronous variant on the context's stream for device-resident inputs and

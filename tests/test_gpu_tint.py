@@ -121,6 +121,7 @@ def test_effective_action_matches_oracle(prof, fermion, mode):
     with wltube.Context(0) as ctx:
         h = ctx.upload(loops)
         act, err, ca, groups = ctx.effective_action(h, fld, F, T, group=128, nrho=nrho)
+        assert ctx.last_launches()[0] >= 3
         ctx.release(h)
     rho, w = rho_rule(prof == "fixflux", nrho, a, mode == 0)
     rho = rho.astype(np.float32).astype(np.float64)  # the kernel's float centre
@@ -138,3 +139,32 @@ def test_effective_action_matches_oracle(prof, fermion, mode):
     if prof == "smooth":
         e = 0.30282212
         assert np.isclose(ca, -2 * np.pi * F * F / (3 * 0.5 * e * e))
+
+
+@pytest.mark.parametrize("prof,fermion", [("smooth", 1), ("gaussian", 0)])
+def test_effective_action_with_the_reference_T_rule(prof, fermion):
+    """The proper-time integral by integrateT's own rule (T = (1 - t)/t, the
+    reference's 40 panels in rhogrand) under the radial integral, against the
+    oracle's integrateT (pinned to the reference's Tint.c by the golden
+    vectors) at every radial node."""
+    import wltube
+
+    loops = O.vloops(10, 512, 128)
+    nrho, F = 2, 1.0
+    fld = wltube.field(prof, fermion=fermion, nint=4, lambda2=0.5)
+    with wltube.Context(0) as ctx:
+        h = ctx.upload(loops)
+        act, err, ca, groups = ctx.effective_action(h, fld, F, None, group=128, nrho=nrho,
+                                                    t_panels=40)
+        ctx.release(h)
+    rho, w = rho_rule(False, nrho, 0.0, True)
+    ofld = O.field(prof, fermion=fermion, nint=4, lambda2=0.5)
+    I = np.array([O.integrateT(loops, 40, float(r), 0.0, F, ofld)[0] for r in rho])  # [rho][g]
+    norm = 1 / (4 * np.pi) if fermion else -1 / (2 * np.pi)
+    ref_g = norm * np.einsum("r,r,rg->g", w, rho, np.where(np.isinf(I), 0.0, I))
+    ref_se = ref_g.std(ddof=1) / np.sqrt(len(ref_g))
+    assert np.isfinite(act) and err > 0
+    # the kernel evaluates W at T' = float(sqrt(T))^2, the oracle at T: both
+    # far inside the Monte Carlo error
+    assert abs(act - ref_g.mean()) <= 0.05 * ref_se + 1e-12
+    np.testing.assert_allclose(groups, ref_g, rtol=0, atol=0.05 * ref_se + 1e-12)

@@ -1061,12 +1061,10 @@ static void log_simpson_weights(const double *T, int n, double du, double *w) {
 // <W> on the (rho, log T) grid, the FP64 proper-time integral per group and
 // the jackknife on the device; results stay there (*ta), the caller copies
 // what it needs and checks the status.
-static int tint_run(wl_ctx *ctx, int handle, const wl_field *field, int nrho,
-                    const double *host_rho, int nT, const double *host_T, int nF,
-                    const double *host_F, int group, int nbins, bool want_igrand,
-                    wl::TintArgs *ta_out) {
-  if (!host_rho || !host_T) return fail(ctx, WL_ERR_INVALID, "NULL rho or T array");
-  if (nrho < 1 || nT < 3) return fail(ctx, WL_ERR_INVALID, "need nrho >= 1 and nT >= 3");
+// Simpson weights (dT) of a log-spaced grid after checking it
+static int log_grid_weights(wl_ctx *ctx, int nT, const double *host_T, std::vector<double> *w) {
+  if (!host_T) return fail(ctx, WL_ERR_INVALID, "NULL T array");
+  if (nT < 3) return fail(ctx, WL_ERR_INVALID, "need nT >= 3");
   const double du = log(host_T[1]) - log(host_T[0]);
   for (int k = 0; k < nT; ++k) {
     if (!(host_T[k] > 0.0) || !isfinite(host_T[k]))
@@ -1075,6 +1073,38 @@ static int tint_run(wl_ctx *ctx, int handle, const wl_field *field, int nrho,
       return fail(ctx, WL_ERR_INVALID, "T must be log-spaced (ascending, uniform in ln T)");
   }
   if (!(du > 0.0)) return fail(ctx, WL_ERR_INVALID, "T must be ascending");
+  w->assign(nT, 0.0);
+  log_simpson_weights(host_T, nT, du, w->data());
+  return WL_OK;
+}
+
+// Nodes and weights (dT) of integrateT's rule (Tint.c:100-175): T = (1 - t)/t,
+// n Simpson panels in t with the Jacobian 1/t^2.  The reference evaluates each
+// panel's right end twice instead of its left end (Tint.c:127-130); summed
+// over the panels that differs from Simpson's rule only by f(t = 1) - f(0),
+// and both vanish (T = 0 and T = infinity), so one rule serves both modes.
+static void tsub_nodes(int n, std::vector<double> *T, std::vector<double> *w) {
+  const double h = 1.0 / n;
+  T->clear();
+  w->clear();
+  for (int i = 0; i < n; ++i) {
+    const double tm = h * (i + 0.5);
+    T->push_back((1.0 - tm) / tm);
+    w->push_back(4.0 * h / 6.0 / (tm * tm));
+    if (i < n - 1) {  // t = 1 (T = 0) contributes 0
+      const double tr = h * (i + 1);
+      T->push_back((1.0 - tr) / tr);
+      w->push_back(2.0 * h / 6.0 / (tr * tr));
+    }
+  }
+}
+
+static int tint_run(wl_ctx *ctx, int handle, const wl_field *field, int nrho,
+                    const double *host_rho, int nT, const double *host_T, const double *host_w,
+                    int nF, const double *host_F, int group, int nbins, bool want_igrand,
+                    wl::TintArgs *ta_out) {
+  if (!host_rho || !host_T || !host_w) return fail(ctx, WL_ERR_INVALID, "NULL rho or T array");
+  if (nrho < 1 || nT < 1) return fail(ctx, WL_ERR_INVALID, "need nrho >= 1 and nT >= 1");
   Ensemble e;
   int kprof;
   FieldDev fd;
@@ -1114,7 +1144,7 @@ static int tint_run(wl_ctx *ctx, int handle, const wl_field *field, int nrho,
   std::vector<double> h((size_t)nrho + 2 * (size_t)nT + nF);
   memcpy(h.data(), host_rho, sizeof(double) * nrho);
   memcpy(h.data() + nrho, host_T, sizeof(double) * nT);
-  log_simpson_weights(host_T, nT, du, h.data() + nrho + nT);
+  memcpy(h.data() + nrho + nT, host_w, sizeof(double) * nT);
   memcpy(h.data() + nrho + 2 * nT, host_F, sizeof(double) * nF);
   WL_CHECK(ctx, cudaMemcpyAsync(ctx->aux.p, h.data(), sizeof(double) * h.size(),
                                 cudaMemcpyHostToDevice, ctx->stream));
@@ -1154,10 +1184,13 @@ int wl_tint(wl_ctx *ctx, int handle, const wl_field *field, int nrho, const doub
             double *out_leff, double *out_err, double *out_igrand) {
   if (!ctx) return WL_ERR_INVALID;
   if (!out_leff || !out_err) return fail(ctx, WL_ERR_INVALID, "NULL output array");
-  wl::TintArgs ta;
-  int r = tint_run(ctx, handle, field, nrho, host_rho, nT, host_T, nF, host_F, group, nbins,
-                   out_igrand != nullptr, &ta);
+  std::vector<double> w;
+  int r = log_grid_weights(ctx, nT, host_T, &w);
   if (r) return r;
+  wl::TintArgs ta;
+  if ((r = tint_run(ctx, handle, field, nrho, host_rho, nT, host_T, w.data(), nF, host_F, group,
+                    nbins, out_igrand != nullptr, &ta)))
+    return r;
   const size_t n_le = (size_t)nrho * nF, n_igr = (size_t)nrho * nF * nT * ta.ng;
   WL_CHECK(ctx, cudaMemcpyAsync(out_leff, ta.leff, sizeof(double) * n_le, cudaMemcpyDeviceToHost,
                                 ctx->stream));
@@ -1194,11 +1227,22 @@ static double classical_action(int profile, double F, double l2, double a, doubl
   }
 }
 
-int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F, int nT,
-                        const double *host_T, int group, int nrho, double *out_action,
+int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F, int t_rule,
+                        int nT, const double *host_T, int group, int nrho, double *out_action,
                         double *out_err, double *out_classical, double *out_groups) {
   if (!ctx) return WL_ERR_INVALID;
   if (!field || !out_action || !out_err) return fail(ctx, WL_ERR_INVALID, "NULL argument");
+  std::vector<double> Tn, Tw;
+  if (t_rule == WL_TRULE_LOG) {
+    int r0 = log_grid_weights(ctx, nT, host_T, &Tw);
+    if (r0) return r0;
+    Tn.assign(host_T, host_T + nT);
+  } else if (t_rule == WL_TRULE_SUBST) {
+    if (nT < 1 || nT > 100000) return fail(ctx, WL_ERR_INVALID, "nT panels must be in [1, 1e5]");
+    tsub_nodes(nT, &Tn, &Tw);
+  } else {
+    return fail(ctx, WL_ERR_INVALID, "unknown proper-time rule %d", t_rule);
+  }
   if (nrho < 1 || nrho > 4096) return fail(ctx, WL_ERR_INVALID, "nrho must be in [1, 4096]");
   if (!isfinite(F)) return fail(ctx, WL_ERR_INVALID, "F is not finite");
   const int p = field->profile;
@@ -1255,8 +1299,8 @@ int wl_effective_action(wl_ctx *ctx, int handle, const wl_field *field, double F
     return fail(ctx, WL_ERR_INVALID, "group %d must divide Nl = %d into at least 2 groups", group,
                 e.Nl);
   wl::TintArgs ta;
-  if ((r = tint_run(ctx, handle, field, nr, rho.data(), nT, host_T, 1, &F, group, e.Nl / group,
-                    false, &ta)))
+  if ((r = tint_run(ctx, handle, field, nr, rho.data(), (int)Tn.size(), Tn.data(), Tw.data(), 1,
+                    &F, group, e.Nl / group, false, &ta)))
     return r;
   std::vector<double> Ig((size_t)nr * ta.ng);
   WL_CHECK(ctx, cudaMemcpyAsync(Ig.data(), ta.Ig, sizeof(double) * Ig.size(),

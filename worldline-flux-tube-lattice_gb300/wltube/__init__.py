@@ -95,6 +95,7 @@ class ServerStats(C.Structure):
 
 
 REQ_W, REQ_LEFF = 0, 1
+TRULE_LOG, TRULE_SUBST = 0, 1
 
 
 class Float4(C.Structure):
@@ -148,8 +149,8 @@ def lib():
                               C.c_int, C.c_int, dp, dp, dp]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
         L.wl_spline_table.argtypes = [C.c_double, C.c_double, C.c_int, fp, fp]
-        L.wl_effective_action.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_int, dp,
-                                          C.c_int, C.c_int, dp, dp, dp, dp]
+        L.wl_effective_action.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_int,
+                                          C.c_int, dp, C.c_int, C.c_int, dp, dp, dp, dp]
         L.wl_batch_eval.argtypes = [vp, C.c_int, C.POINTER(Job), C.c_int]
         L.wl_batch_autotune.argtypes = [vp, C.c_int, C.POINTER(Job), ip, ip]
         L.wl_batch_stats.argtypes = [vp, dp, ip, ip, ip]
@@ -330,18 +331,24 @@ class Context:
                                   _p(ig, C.c_double) if want_igrand else None))
         return leff, err, ig
 
-    def effective_action(self, handle: int, fld: Field, F: float, T, group: int = 128,
-                         nrho: int = 20):
+    def effective_action(self, handle: int, fld: Field, F: float, T=None, group: int = 128,
+                         nrho: int = 20, t_panels: int = 40):
         """wl_effective_action: (mean, standard error, classical action,
-        per-group values) of the effective action per unit length."""
-        T = _d(T)
+        per-group values) of the effective action per unit length.  T: a
+        log-spaced grid (Simpson in ln T); None: integrateT's t-substitution
+        with t_panels panels, as the reference's rhogrand (40)."""
         Nl = C.c_int()
         self._check(lib().wl_ensemble_info(self._h, handle, None, C.byref(Nl), None))
         groups = np.empty(Nl.value // group)
         a, e, ca = C.c_double(), C.c_double(), C.c_double()
-        self._check(lib().wl_effective_action(self._h, handle, C.byref(fld), float(F), len(T),
-                                              _p(T, C.c_double), group, nrho, C.byref(a),
-                                              C.byref(e), C.byref(ca), _p(groups, C.c_double)))
+        if T is None:
+            rule, n, Tp = TRULE_SUBST, t_panels, None
+        else:
+            T = _d(T)
+            rule, n, Tp = TRULE_LOG, len(T), _p(T, C.c_double)
+        self._check(lib().wl_effective_action(self._h, handle, C.byref(fld), float(F), rule, n,
+                                              Tp, group, nrho, C.byref(a), C.byref(e),
+                                              C.byref(ca), _p(groups, C.c_double)))
         return a.value, e.value, ca.value, groups
 
     def _jobs(self, jobs):
