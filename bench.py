@@ -515,6 +515,41 @@ def run_lattice(args):
     ctx.close()
 
 
+def run_effact(args):
+    """The reference driver's own run (EffAct.c:300-520, its main): the
+    effective action of a smooth tube (F = 1, lambda = lmin = 0.1 a, a = 1)
+    in scalar QED on Nl = 5120 loops of Nppl = 1024 points, 40 groups of 128,
+    the radial rule with 20 panels and integrateT's rule with 40 panels
+    (EffAct.c:22, 484) at the reference kernel's 50 Simpson intervals --
+    through wl_effective_action, timed end to end per call."""
+    import wltube
+
+    Nl, ppl = 5120, 1024
+    ctx = wltube.Context(0)
+    h = ctx.generate(SEED, Nl, ppl)
+    fld = wltube.field("smooth", fermion=0, nint=50, lambda2=0.01)
+    ctx.effective_action(h, fld, 1.0, None, group=128, nrho=20, t_panels=40)  # warm-up
+    times, out = [], None
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        out = ctx.effective_action(h, fld, 1.0, None, group=128, nrho=20, t_panels=40)
+        times.append(time.perf_counter() - t0)
+    ninst = 2 * 20 * (2 * 40 - 1)  # radial nodes x proper-time nodes
+    segs = ninst * Nl * ppl
+    sec = float(np.median(times))
+    print(json.dumps({
+        "metric": "effective action per call (the reference driver's configuration)",
+        "value": sec, "unit": "s", "higher_is_better": False,
+        "segments_per_call": segs, "segments_per_s": segs / sec,
+        "instances": ninst, "effective_action": out[0], "standard_error": out[1],
+        "classical_action": out[2], "steps": len(times),
+        "config": {"workload": "EffAct main: smooth, scalar, F=1, lambda^2=0.01, Nl=5120 x "
+                               "Nppl=1024 (seed 2), 40 groups, rho rule 20 panels, integrateT "
+                               "rule 40 panels, 50 Simpson intervals"}}))
+    ctx.release(h)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -526,7 +561,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 128 instances on the full ensemble, no e2e/cpu")
-    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "serve", "lattice"],
+    ap.add_argument("--workload", default="c2",
+                    choices=["c2", "batch", "serve", "lattice", "effact"],
                     help="c2: the headline spinor workload; batch: uneven multi-job batch; "
                          "serve: Poisson request stream through the server")
     ap.add_argument("--jobs", type=int, default=32, help="jobs of the batch workload")
@@ -553,6 +589,9 @@ def main():
         return
     if args.workload == "lattice":
         run_lattice(args)
+        return
+    if args.workload == "effact":
+        run_effact(args)
         return
     world, rank, local = dist_setup()
     if args.impl == "reference":
