@@ -14,39 +14,43 @@ namespace wl {
 
 namespace {
 
-// One tile of a job: packed pairs (256 instances) for the light profiles at 4
-// intervals, one instance per thread otherwise -- the split the single-job
-// sweep makes (sweep_pairs), so a job's results match it bit for bit.
+// One tile of a job: packed pairs (256 instances) for the light profiles at
+// 4 intervals -- as the single-job sweep, so such a job's results match it bit
+// for bit -- one instance per thread otherwise (sweep_tile_instances).
 template <bool FERM, int NINT>
 __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, int chunk,
                                          const SweepShared &S, double (*sacc2)[kPairTile],
                                          int &consumed) {
-  if constexpr (NINT == 4) {
+  if constexpr (NINT != 4) {
     switch (kprof) {
-      case kSmooth:
-        sweep_tile2<kSmooth, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring, consumed);
-        return;
-      case kGaussian:
-        sweep_tile2<kGaussian, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
-                                        consumed);
-        return;
-      case kStep:
-        sweep_tile2<kStep, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring, consumed);
-        return;
-      case kQuadratic:
-        sweep_tile2<kQuadratic, FERM, 4>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
-                                         consumed);
-        return;
+      case kSmooth: sweep_tile<kSmooth, FERM, NINT>(A, tx, chunk, S, consumed); break;
+      case kGaussian: sweep_tile<kGaussian, FERM, NINT>(A, tx, chunk, S, consumed); break;
+      case kStep: sweep_tile<kStep, FERM, NINT>(A, tx, chunk, S, consumed); break;
+      case kQuadratic: sweep_tile<kQuadratic, FERM, NINT>(A, tx, chunk, S, consumed); break;
+      case kLattice: sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed); break;
       default: break;
     }
-  }
-  switch (kprof) {
-    case kSmooth: sweep_tile<kSmooth, FERM, NINT>(A, tx, chunk, S, consumed); break;
-    case kGaussian: sweep_tile<kGaussian, FERM, NINT>(A, tx, chunk, S, consumed); break;
-    case kStep: sweep_tile<kStep, FERM, NINT>(A, tx, chunk, S, consumed); break;
-    case kQuadratic: sweep_tile<kQuadratic, FERM, NINT>(A, tx, chunk, S, consumed); break;
-    case kLattice: sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed); break;
-    default: break;
+  } else {
+    switch (kprof) {
+      case kSmooth:
+        sweep_tile2<kSmooth, FERM, NINT>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
+                                         consumed);
+        break;
+      case kGaussian:
+        sweep_tile2<kGaussian, FERM, NINT>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
+                                           consumed);
+        break;
+      case kStep:
+        sweep_tile2<kStep, FERM, NINT>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
+                                       consumed);
+        break;
+      case kQuadratic:
+        sweep_tile2<kQuadratic, FERM, NINT>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
+                                            consumed);
+        break;
+      case kLattice: sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed); break;
+      default: break;
+    }
   }
 }
 

@@ -49,15 +49,16 @@ struct SweepArgs {
   const int *perm;
 };
 
-// Instances per tile of the sweep: the light profiles at 4 Simpson intervals
-// run two instances per thread as packed f32x2 pairs (256 per CTA of 128
-// threads), everything else one per thread.
-inline __host__ __device__ bool sweep_pairs(int kprof, int nint) {
-  return nint == 4 &&
-         (kprof == kSmooth || kprof == kStep || kprof == kQuadratic || kprof == kGaussian);
+// The single-job sweep runs the light profiles two instances per thread as
+// packed f32x2 pairs (256 per CTA of 128 threads), the lattice and the heavy
+// profiles one per thread.  The persistent batch kernel does the same for
+// 4 intervals only (a second, run-time-interval pair path would push its
+// registers over the 4-CTA budget): instances per batch tile.
+inline __host__ __device__ bool light_profile(int kprof) {
+  return kprof == kSmooth || kprof == kStep || kprof == kQuadratic || kprof == kGaussian;
 }
 inline __host__ __device__ int sweep_tile_instances(int kprof, int nint) {
-  return sweep_pairs(kprof, nint) ? 2 * kSweepThreads : kSweepThreads;
+  return (nint == 4 && light_profile(kprof)) ? 2 * kSweepThreads : kSweepThreads;
 }
 
 // Persistent multi-job sweep: a queue of tiles (job, instance tile, loop

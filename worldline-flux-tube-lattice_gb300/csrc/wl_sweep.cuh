@@ -473,8 +473,8 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
   const dim3 grid((a.ninst + kSweepThreads - 1) / kSweepThreads, a.n_chunks);
   const size_t smem = sweep_smem_bytes();
   if constexpr (P == kSmooth || P == kStep || P == kQuadratic || P == kGaussian) {
-    const dim3 grid2((a.ninst + kPairTile - 1) / kPairTile, a.n_chunks);
-    if (sweep_pairs(P, nint)) {  // packed pairs
+    if (nint == 4) {  // packed pairs
+      const dim3 grid2((a.ninst + kPairTile - 1) / kPairTile, a.n_chunks);
       if (fermion)
         sweep2_kernel<P, true, 4><<<grid2, kSweepThreads, smem, s>>>(a);
       else
@@ -482,12 +482,16 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
       return cudaGetLastError();
     }
   }
+  // one instance per thread: other interval counts (50 unrolled: the
+  // reference's; others at run time -- a run-time-interval pair kernel
+  // measured 26 % slower than the unrolled 50), the lattice at 4 too, and the
+  // heavy profiles
 #define WL_SWEEP_CASE(FE, NI)                                                      \
   if (fermion == FE && (NI == 0 || nint == NI)) {                                  \
     sweep_kernel<P, FE, NI><<<grid, kSweepThreads, smem, s>>>(a);                  \
     return cudaGetLastError();                                                     \
   }
-  if constexpr (!Profile<P>::kHeavy) {
+  if constexpr (P == kLattice) {
     WL_SWEEP_CASE(true, 4)
     WL_SWEEP_CASE(false, 4)
   }
