@@ -117,3 +117,49 @@ def test_argument_limits(ctx):
             ctx.upload(O.vloops(34, 8, 64)[:, :30])
     finally:
         ctx.release(h)
+
+
+def test_pure_gauge_winding_phase_on_the_gpu(ctx):
+    """Circles about a step tube (f = 1 on them): every sub-loop's phase is
+    2 pi F n for n windings (exact mode; see the oracle's known answer)."""
+    import wltube
+
+    for windings in (1, 2, -1):
+        k = np.arange(1024)
+        ang = 2.0 * np.pi * windings * k / 1024
+        L = np.zeros((8, 1024, 4), np.float32)
+        L[:, :, 0] = 3.0 * np.cos(ang)
+        L[:, :, 1] = 3.0 * np.sin(ang)
+        h = ctx.upload(L)
+        try:
+            s, _ = ctx.loops(h, wltube.field("step", nint=8, mode=1, lambda2=1.0), 0.0, 0.0, 1.0,
+                             0.7)
+        finally:
+            ctx.release(h)
+        np.testing.assert_allclose(s[:, :3], 2 * np.pi * 0.7 * windings, rtol=2e-6)
+
+
+def test_nan_loop_poisons_only_its_group(ctx):
+    """A loop with a NaN point (an injected bad input the library does not
+    scan for on the device, as the reference does not) makes its group's <W>
+    NaN; the other groups, the status and later calls are unaffected."""
+    import wltube
+
+    loops = O.vloops(35, 512, 64)
+    loops[300, 17, 0] = np.nan          # loop 300: group 2 of 128-loop groups
+    cx, cy, T = f32_exact(np.linspace(0, 2, 48), np.zeros(48), np.geomspace(0.05, 2.0, 48))
+    fld = wltube.field("smooth", fermion=1, nint=4)
+    h = ctx.upload(loops)
+    try:
+        g, mean, sem = ctx.eval(h, fld, cx, cy, T, [1.0])
+        assert np.all(np.isnan(g[:, 0, 2]))
+        assert np.all(np.isfinite(g[:, 0, [0, 1, 3]]))
+        assert np.all(np.isnan(mean))
+        clean = O.vloops(35, 512, 64)
+        h2 = ctx.upload(clean)
+        g2, _, _ = ctx.eval(h2, fld, cx, cy, T, [1.0])
+        ctx.release(h2)
+        assert np.all(np.isfinite(g2))
+        np.testing.assert_array_equal(g2[:, 0, [0, 1, 3]], g[:, 0, [0, 1, 3]])
+    finally:
+        ctx.release(h)

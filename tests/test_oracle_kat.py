@@ -112,3 +112,31 @@ def test_lattice_image_selection_matches_full_sum():
             assert np.abs(f_cut - f_all).max() < 1e-6 * max(np.abs(f_all).max(), 1.0), (a, T)
     finally:
         O.set_lattice_rcut(O.LATTICE_RCUT_L)
+
+
+def circle_loops(n_points, radius, windings):
+    """Closed polygons on a circle about the origin (float4 points, z = w = 0)."""
+    k = np.arange(n_points)
+    ang = 2.0 * np.pi * windings * k / n_points
+    L = np.zeros((1, n_points, 4), np.float32)
+    L[0, :, 0] = radius * np.cos(ang)
+    L[0, :, 1] = radius * np.sin(ang)
+    return L
+
+
+def test_pure_gauge_winding_phase():
+    """Outside a step tube f = 1: A is pure gauge and every closed sub-loop
+    that winds n times around the tube picks up the phase 2 pi F n (the
+    scope table's winding known answer) -- in exact mode.  The reference's
+    clamp b >= 1e-8 (intEV.cu:420) replaces the negative b of every chord of
+    a circle about the origin, so in ref-compat mode the phase falls short
+    (2 pi (1 - 7.5e-5) for the N/2 loop of 1024 points)."""
+    for windings in (1, 2, -1):
+        L = circle_loops(1024, 3.0, windings)
+        for F in (0.3, 1.0):
+            s, _ = O.loops_phases(L, 0.0, 0.0, 1.0, F,
+                                  O.field("step", lambda2=1.0, nint=8, mode=1))
+            np.testing.assert_allclose(s[0], 2 * np.pi * F * windings, rtol=1e-9)
+    s, _ = O.loops_phases(circle_loops(1024, 3.0, 1), 0.0, 0.0, 1.0, 1.0,
+                          O.field("step", lambda2=1.0, nint=8, mode=0))
+    assert 1e-5 < 1 - s[0, 0] / (2 * np.pi) < 1e-4
