@@ -170,3 +170,52 @@ def test_invalid_requests_are_refused_at_submit():
             srv.submit_leff(1, 256, 64, fld, [0.0], [0.1, 0.2, 0.4, 0.5], [1.0], nbins=2)
         st = srv.stats()
     assert st["submitted"] == 0
+
+
+def test_many_concurrent_requests_equal_alone():
+    """Forty small requests submitted from two host threads while earlier ones
+    run: each result equals the request evaluated alone, bit for bit."""
+    import threading
+
+    import wltube
+
+    rng = np.random.default_rng(77)
+    profs = ["smooth", "gaussian", "step", "quadratic"]
+    reqs = []
+    for i in range(40):
+        prof = profs[i % 4]
+        Nl = int(rng.choice([256, 512]))
+        ppl = int(rng.choice([64, 128, 256]))
+        n = int(rng.integers(1, 300))
+        cx, cy, T = f32_exact(rng.uniform(0, 2, n), rng.uniform(-0.2, 0.2, n),
+                              np.exp(rng.uniform(np.log(0.05), np.log(2.0), n)))
+        reqs.append(dict(seed=int(rng.integers(60, 64)), Nl=Nl, ppl=ppl, cx=cx, cy=cy, T=T,
+                         F=[float(rng.uniform(0.2, 1.5))],
+                         fld=wltube.field(prof, fermion=i % 2, nint=4, lambda2=1.0)))
+    tickets = [None] * len(reqs)
+    with wltube.Server(0, quantum_ms=1.0, max_requests=8) as srv:
+        def submit(part):
+            for i in part:
+                r = reqs[i]
+                tickets[i] = srv.submit_w(r["seed"], r["Nl"], r["ppl"], r["fld"], r["cx"], r["cy"],
+                                          r["T"], r["F"], want_groups=True)
+        th = [threading.Thread(target=submit, args=(range(k, 40, 2),)) for k in (0, 1)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        served = [done(srv, t) for t in tickets]
+        st = srv.stats()
+    assert st["completed"] == 40 and st["failed"] == 0
+    with wltube.Context(0) as ctx:
+        handles = {}
+        for r, (g, m, s) in zip(reqs, served):
+            key = (r["seed"], r["Nl"], r["ppl"])
+            if key not in handles:
+                handles[key] = ctx.generate(*key)
+            (g1, m1, s1), = ctx.batch_eval([{"handle": handles[key], "field": r["fld"],
+                                             "cx": r["cx"], "cy": r["cy"], "T": r["T"],
+                                             "F": r["F"], "group": 128}], graph=False)
+            assert np.array_equal(g, g1) and np.array_equal(m, m1) and np.array_equal(s, s1)
+        for h in handles.values():
+            ctx.release(h)
