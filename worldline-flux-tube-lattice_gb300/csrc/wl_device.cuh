@@ -31,6 +31,21 @@ __device__ __forceinline__ float expneg_fast(float x) {
   return ex2_fast(-1.4426950408889634f * x);
 }
 
+// 1/d for a positive normal d on the FP32 pipe instead of the MUFU: the
+// bit-level initial approximation (integer subtraction from the exponent and
+// mantissa bits, Blinn, "Floating-point tricks", IEEE CG&A 17(4), 1997; the
+// constant 0x7ef311c2 is the minimax fit of the relative error over two
+// binades, 5.1e-2), one Newton-Raphson step x(1 + e) and one third-order step
+// x(1 + e + e^2), e = 1 - d x: error 5.1e-2 -> 2.6e-3 -> 1.7e-8, i.e. within
+// 0.78 ulp of 1/d (tests/test_device_math.py).  NaN in, NaN out.
+__device__ __forceinline__ float rcp_newton(float d) {
+  float x = __int_as_float(0x7ef311c2 - __float_as_int(d));
+  float e = fmaf(-d, x, 1.0f);
+  x = fmaf(x, e, x);
+  e = fmaf(-d, x, 1.0f);
+  return fmaf(x, fmaf(e, e, e), x);
+}
+
 // (1 - e^-x) / x for 0 <= x < 0.5: a degree-5 polynomial fitted to the
 // function on [0, 0.5] (iteratively reweighted least squares for the relative
 // error on Chebyshev nodes); FP32 Horner evaluation stays within 5.5e-8 of it,
@@ -259,6 +274,41 @@ __device__ __forceinline__ float profile_shift(const FieldDev &F) {
     return 0.0f;
 }
 
+// The smooth profile at a fixed interval count of 8 or more: one node costs
+// 1 MUFU reciprocal against 3 (scalar) or 5 (spinor) FP32 operations, so the
+// MUFU (16 per SM per clock, an eighth of the FP32 rate) bounds the segment
+// alone.  Every kSoftRcp-th interior node takes its reciprocal from
+// rcp_newton (5 FP32 + 1 integer operation) to share the work between the
+// two pipes; 0 = every node on the MUFU.
+// Periods measured on the GB300 at 50 intervals: one instance per thread,
+// scalar 5 (+16 % over no FP32-pipe reciprocal), spinor 12 (+5 %); packed
+// pairs, scalar 4 (+20 %), spinor 3 (+13 %).  More FP32-pipe reciprocals
+// measured slower: the segment then runs out of issue slots and latency
+// hiding before either pipe saturates.
+#ifndef WL_SOFT_RCP_SCALAR
+#define WL_SOFT_RCP_SCALAR 5
+#endif
+#ifndef WL_SOFT_RCP_SPINOR
+#define WL_SOFT_RCP_SPINOR 12
+#endif
+#ifndef WL_SOFT_RCP_PAIR_SCALAR
+#define WL_SOFT_RCP_PAIR_SCALAR 4
+#endif
+#ifndef WL_SOFT_RCP_PAIR_SPINOR
+#define WL_SOFT_RCP_PAIR_SPINOR 3
+#endif
+template <int P, bool FERM, int NINT, bool PAIR = false>
+constexpr int soft_rcp_period() {
+  if constexpr (P == kSmooth && NINT >= 8) {
+    if constexpr (PAIR)
+      return FERM ? WL_SOFT_RCP_PAIR_SPINOR : WL_SOFT_RCP_PAIR_SCALAR;
+    else
+      return FERM ? WL_SOFT_RCP_SPINOR : WL_SOFT_RCP_SCALAR;
+  } else {
+    return 0;
+  }
+}
+
 // ------------------------------------------------------------- segment --
 // One segment z_i -> z_j of a sub-loop (intEV.cu:526-552 with Idt,
 // intEV.cu:408-459): rho^2(t) = a + 2bt + ct^2 with a = |z_i|^2,
@@ -290,11 +340,17 @@ __device__ __forceinline__ void segment(float zix, float ziy, float zjx, float z
   Profile<P>::eval(as, F, g0, f0);
   Profile<P>::eval(ae, F, g1, f1);
   float so = 0.0f, se = 0.0f, fo = 0.0f, fe = 0.0f;
+  constexpr int kSoftRcp = soft_rcp_period<P, FERM, NINT>();
   auto node = [&](int j, float t) {
     float r2 = fmaf(fmaf(c, t, b2), t, as);
     if (kFloor) r2 = fmaxf(r2, F.clampI);
     float g, fp;
-    Profile<P>::eval(r2, F, g, fp);
+    if (kSoftRcp > 0 && j % kSoftRcp == kSoftRcp - 1) {  // j is a constant after unrolling
+      g = rcp_newton(r2);
+      fp = g * g;
+    } else {
+      Profile<P>::eval(r2, F, g, fp);
+    }
     if (j & 1) {
       so += g;
       if (FERM) fo += fp;
@@ -331,6 +387,16 @@ __device__ __forceinline__ float2 max2(float2 a, float b) {
   return make_float2(fmaxf(a.x, b), fmaxf(a.y, b));
 }
 __device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcp_fast(a.x), rcp_fast(a.y)); }
+// rcp_newton on a pair: the seeds per half, the refinement as packed FMAs
+__device__ __forceinline__ float2 rcp_newton2(float2 d) {
+  const float2 nd = neg2(d);
+  float2 x = make_float2(__int_as_float(0x7ef311c2 - __float_as_int(d.x)),
+                         __int_as_float(0x7ef311c2 - __float_as_int(d.y)));
+  float2 e = fma2(nd, x, f2(1.0f));
+  x = fma2(x, e, x);
+  e = fma2(nd, x, f2(1.0f));
+  return fma2(x, fma2(e, e, e), x);
+}
 
 // the light profiles on a pair: g = f/rho^2 and fp = f'/fp_scale as in eval
 template <int P>
@@ -364,6 +430,7 @@ template <int P, bool FERM, int NINT>
 __device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, float2 zjy,
                                          const FieldDev &F, float2 &ph, float2 &sp) {
   static_assert(!Profile<P>::kHeavy && NINT > 0, "pairs: light profiles, fixed intervals");
+  constexpr int kSoftRcp = soft_rcp_period<P, FERM, NINT, true>();
   const float2 dx = add2(zjx, neg2(zix)), dy = add2(zjy, neg2(ziy));
   float2 a = fma2(zix, zix, mul2(ziy, ziy));
   float2 b = fma2(zix, dx, mul2(ziy, dy));
@@ -384,7 +451,12 @@ __device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, flo
     const float t = (float)j * (1.0f / (float)NINT);
     const float2 r2 = fma2(fma2(c, f2(t), b2), f2(t), as);
     float2 g, fp;
-    eval2<P>(r2, F, g, fp);
+    if (kSoftRcp > 0 && j % kSoftRcp == kSoftRcp - 1) {  // smooth only: g = 1/(l2 + rho^2)
+      g = rcp_newton2(r2);
+      fp = mul2(g, g);
+    } else {
+      eval2<P>(r2, F, g, fp);
+    }
     if (j & 1) {
       so = add2(so, g);
       if (FERM) fo = add2(fo, fp);
@@ -396,6 +468,32 @@ __device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, flo
   const float2 S = fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(g0, g1)));
   ph = fma2(xyyx, S, ph);
   if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(f0, f1))));
+}
+
+// segment2 as a called function for many intervals: one copy of the long
+// node sequence instead of one per call site of the sweep (a dozen), which
+// keeps the kernel within the instruction cache; the sums travel by value
+#ifndef WL_SEG2_CALL_MIN
+#define WL_SEG2_CALL_MIN 8
+#endif
+template <int P, bool FERM, int NINT>
+__device__ __noinline__ float4 segment2_called(float2 zix, float2 ziy, float2 zjx, float2 zjy,
+                                               const FieldDev &F, float4 acc) {
+  float2 ph = make_float2(acc.x, acc.y), sp = make_float2(acc.z, acc.w);
+  segment2<P, FERM, NINT>(zix, ziy, zjx, zjy, F, ph, sp);
+  return make_float4(ph.x, ph.y, sp.x, sp.y);
+}
+template <int P, bool FERM, int NINT>
+__device__ __forceinline__ void seg2(float2 zix, float2 ziy, float2 zjx, float2 zjy,
+                                     const FieldDev &F, float2 &ph, float2 &sp) {
+  if constexpr (NINT >= WL_SEG2_CALL_MIN) {
+    const float4 r = segment2_called<P, FERM, NINT>(zix, ziy, zjx, zjy, F,
+                                                    make_float4(ph.x, ph.y, sp.x, sp.y));
+    ph = make_float2(r.x, r.y);
+    sp = make_float2(r.z, r.w);
+  } else {
+    segment2<P, FERM, NINT>(zix, ziy, zjx, zjy, F, ph, sp);
+  }
 }
 
 __device__ __forceinline__ void kahan_add2(float2 &sum, float2 &comp, float2 x) {
@@ -417,6 +515,7 @@ struct Profile<kLattice> {  // spin integrand f' = e^{-x}/l2, x = rho^2/l2
 
 struct ImgRange {
   int m0, m1, n0, n1;
+  int inside;  // the whole range lies in the disk m^2 + n^2 <= (rimage/a)^2
 };
 
 __device__ __forceinline__ ImgRange image_range(float4 bb, float s, float cx, float cy,
@@ -428,6 +527,8 @@ __device__ __forceinline__ ImgRange image_range(float4 bb, float s, float cx, fl
   r.m1 = min(lim, (int)floorf((fmaf(s, bb.y, cx) + F.rcut) * inva));
   r.n0 = max(-lim, (int)ceilf((fmaf(s, bb.z, cy) - F.rcut) * inva));
   r.n1 = min(lim, (int)floorf((fmaf(s, bb.w, cy) + F.rcut) * inva));
+  const int mx = max(abs(r.m0), abs(r.m1)), nx = max(abs(r.n0), abs(r.n1));
+  r.inside = (float)(mx * mx) + (float)(nx * nx) <= F.rimg2;
   return r;
 }
 
@@ -472,10 +573,8 @@ __device__ __noinline__ float2 segment_lattice(float zix, float ziy, float zjx, 
   const float cs = fmaf(dx, dx, dy * dy) * il2;
   const int nint = NINT > 0 ? NINT : F.nint;
   const float h = NINT > 0 ? 1.0f / (float)NINT : F.h;
-  // the whole range inside the disk m^2 + n^2 <= (rimage/a)^2 (the usual
-  // case): no per-row trimming
-  const int mx = max(abs(img.m0), abs(img.m1)), nx = max(abs(img.n0), abs(img.n1));
-  const bool inside = (float)(mx * mx) + (float)(nx * nx) <= F.rimg2;
+  // the whole range inside the disk (the usual case): no per-row trimming
+  const bool inside = img.inside;
   for (int m = img.m0; m <= img.m1; ++m) {
     const float ux = fmaf(-(float)m, F.a, zix);
     const float mm = (float)(m * m);

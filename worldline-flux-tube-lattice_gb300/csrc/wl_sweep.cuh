@@ -89,7 +89,7 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
   // previous point of each sub-loop and the first points (closing segments)
   float zAx = 0.f, zAy = 0.f, zBx = 0.f, zBy = 0.f, zOx = 0.f, zOy = 0.f;
   float z0x = 0.f, z0y = 0.f, z1x = 0.f, z1y = 0.f, z2x = 0.f, z2y = 0.f;
-  ImgRange img = {0, -1, 0, -1};  // lattice images of the current loop
+  ImgRange img = {0, -1, 0, -1, 1};  // lattice images of the current loop
 
   int k = 0;
   for (; k < K; ++k) {
@@ -275,7 +275,7 @@ __device__ __forceinline__ bool sweep_tile2(const SweepArgs &A, int tile_x, int 
       pt(1, z1x, z1y);
       pt(2, z2x, z2y);
       pt(3, z3x, z3y);
-      segment2<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, ph[0], sp[0]);
+      seg2<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, ph[0], sp[0]);
       zAx = z0x; zAy = z0y;
       zBx = z2x; zBy = z2y;
       zOx = z3x; zOy = z3y;
@@ -292,10 +292,10 @@ __device__ __forceinline__ bool sweep_tile2(const SweepArgs &A, int tile_x, int 
         pt(4 * q + 1, P1x, P1y);
         pt(4 * q + 2, P2x, P2y);
         pt(4 * q + 3, P3x, P3y);
-        segment2<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, bp2, bs2);
-        segment2<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, bp0, bs0);
-        segment2<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, bp1, bs1);
-        segment2<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, bp0, bs0);
+        seg2<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, bp2, bs2);
+        seg2<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, bp0, bs0);
+        seg2<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, bp1, bs1);
+        seg2<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, bp0, bs0);
         zAx = P0x; zAy = P0y;
         zBx = P2x; zBy = P2y;
         zOx = P3x; zOy = P3y;
@@ -312,9 +312,9 @@ __device__ __forceinline__ bool sweep_tile2(const SweepArgs &A, int tile_x, int 
     if (c == nck - 1) {
       float2 tp0 = f2(0.f), tp1 = f2(0.f), tp2 = f2(0.f), ts0 = f2(0.f), ts1 = f2(0.f),
              ts2 = f2(0.f);
-      segment2<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, tp0, ts0);
-      segment2<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, tp1, ts1);
-      segment2<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, tp2, ts2);
+      seg2<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, tp0, ts0);
+      seg2<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, tp1, ts1);
+      seg2<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, tp2, ts2);
       kahan_add2(ph[0], pc[0], tp0);
       kahan_add2(ph[1], pc[1], tp1);
       kahan_add2(ph[2], pc[2], tp2);
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kLoopWarps * 32)
   // group q covers points 4q..4q+3 and the four segments ending there; the
   // previous points of group 0 wrap to the end of the loop (closing segments)
   const int nq = A.ppl >> 2;
-  ImgRange img = {0, -1, 0, -1};
+  ImgRange img = {0, -1, 0, -1, 1};
   if constexpr (P == kLattice) img = image_range(A.bbox[l], s, cx, cy, F);
   float ph[3] = {0.f, 0.f, 0.f}, sp[3] = {0.f, 0.f, 0.f};
   for (int q = lane; q < nq; q += 32) {
@@ -472,9 +472,9 @@ template <int P>
 cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStream_t s) {
   const dim3 grid((a.ninst + kSweepThreads - 1) / kSweepThreads, a.n_chunks);
   const size_t smem = sweep_smem_bytes();
+  const dim3 grid2((a.ninst + kPairTile - 1) / kPairTile, a.n_chunks);
   if constexpr (P == kSmooth || P == kStep || P == kQuadratic || P == kGaussian) {
     if (nint == 4) {  // packed pairs
-      const dim3 grid2((a.ninst + kPairTile - 1) / kPairTile, a.n_chunks);
       if (fermion)
         sweep2_kernel<P, true, 4><<<grid2, kSweepThreads, smem, s>>>(a);
       else
@@ -482,10 +482,23 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
       return cudaGetLastError();
     }
   }
-  // one instance per thread: other interval counts (50 unrolled: the
-  // reference's; others at run time -- a run-time-interval pair kernel
-  // measured 26 % slower than the unrolled 50), the lattice at 4 too, and the
-  // heavy profiles
+#ifndef WL_SMOOTH50_PAIRS
+#define WL_SMOOTH50_PAIRS 1
+#endif
+  if constexpr (P == kSmooth && WL_SMOOTH50_PAIRS) {
+    if (nint == 50) {  // the reference's interval count: packed pairs, a share
+                       // of the reciprocals on the FP32 pipe
+      if (fermion)
+        sweep2_kernel<P, true, 50><<<grid2, kSweepThreads, smem, s>>>(a);
+      else
+        sweep2_kernel<P, false, 50><<<grid2, kSweepThreads, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
+  // one instance per thread: other interval counts (50 unrolled for the
+  // other light profiles; others at run time -- a run-time-interval pair
+  // kernel measured 26 % slower than the unrolled 50), the lattice at 4 too,
+  // and the heavy profiles
 #define WL_SWEEP_CASE(FE, NI)                                                      \
   if (fermion == FE && (NI == 0 || nint == NI)) {                                  \
     sweep_kernel<P, FE, NI><<<grid, kSweepThreads, smem, s>>>(a);                  \
