@@ -236,7 +236,7 @@ int wl_last_launches(wl_ctx *ctx, int *launches, const char **sweep_kind);
 /* One evaluation job of a batch: instances of one ensemble and field. */
 typedef struct {
   int handle;            /* ensemble                                         */
-  wl_field field;        /* step, smooth, quadratic or gaussian profile      */
+  wl_field field;        /* any profile (see wl_batch_eval)                  */
   int ninst;             /* instances (host arrays of ninst doubles)         */
   const double *cx, *cy, *T;
   int nF;                /* flux values (<= 4)                               */
@@ -254,7 +254,10 @@ typedef struct {
  * batch (the tile shape depends only on the job and the tuned parameters).
  * The loops per tile come from the context's tuned points-per-tile target
  * (wl_batch_autotune; default 16384), the persistent grid from its tuned CTAs
- * per SM (default: the occupancy limit). */
+ * per SM (default: the occupancy limit).  Jobs of the periodic, spline and
+ * fixflux profiles are not tiles of the persistent kernel: each runs as one
+ * launch of its profile's sweep kernel after it, with the same loops per
+ * tile and partial-sum layout, before the common reduction. */
 int wl_batch_eval(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags);
 
 /* Autotuner: times the batch for every candidate (points per tile in
@@ -333,7 +336,9 @@ typedef struct {
  * admitted request is cut into (instance tile, loop chunk) tiles; each launch
  * of the persistent kernel takes about quantum_ms of tiles from all admitted
  * requests, oldest first, and two launches are kept in flight on two streams
- * so that new requests' work overlaps the tail of the running one.  Results
+ * so that new requests' work overlaps the tail of the running one (periodic,
+ * spline and fixflux requests take whole loop chunks per quantum, launched
+ * as their profile's sweep over that chunk range).  Results
  * of a WL_REQ_W request are bit-identical to wl_batch_eval of the request
  * alone with the same points_per_tile; a WL_REQ_LEFF request integrates
  * those <W> values over proper time as wl_tint does. */

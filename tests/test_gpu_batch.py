@@ -78,3 +78,38 @@ def test_autotune_and_plain_baseline(setup):
                                  j["F"])
     assert ms > 0 and ctx.last_launches() == (21, "plain-per-instance")
     assert werr(g, outs[0][0][:20]) < W_TOL
+
+
+def test_heavy_profiles_in_a_batch(setup):
+    """Periodic, spline and both fixflux variants batch beside the persistent
+    kernel (one sweep launch each, the same partial-sum layout): results
+    equal wl_eval within W_TOL and the FP64 oracle on a few instances, and a
+    job alone in a batch equals it in the mix bit for bit."""
+    import wltube
+
+    ctx, jobs, ens = setup
+    rng = np.random.default_rng(9)
+    heavy = []
+    for prof, fe, ffv, a in [("periodic", 1, 0, 1.0), ("spline", 0, 0, 2.0),
+                             ("fixflux", 0, 0, 2.0), ("fixflux", 1, 1, 2.0)]:
+        n = 20
+        cx, cy, T = f32_exact(rng.uniform(0, 2 * a, n), rng.uniform(-0.2, 0.2, n),
+                              np.exp(rng.uniform(np.log(0.02), np.log(2.0), n)))
+        kw = dict(fermion=fe, nint=8, lambda2=0.5, tubedist=a, ff_variant=ffv)
+        heavy.append({"handle": ens[(64, 256)], "field": wltube.field(prof, **kw), "cx": cx,
+                      "cy": cy, "T": T, "F": [1.0], "group": 128, "ofield": O.field(prof, **kw),
+                      "name": "%s/%d" % (prof, ffv)})
+    outs = ctx.batch_eval([jobs[0]] + heavy, graph=True)
+    assert ctx.last_launches() == (2 + len(heavy), "persistent-batch")
+    loops = ctx.download(ens[(64, 256)])
+    idx = [0, 7, 19]
+    for j, (g, m, s) in zip(heavy, outs[1:]):
+        g1, _, _ = ctx.eval(j["handle"], j["field"], j["cx"], j["cy"], j["T"], j["F"])
+        assert werr(g, g1) < W_TOL, j["name"]
+        ref, S = O.eval_groups(loops, j["cx"][idx], j["cy"][idx], j["T"][idx], j["F"],
+                               j["ofield"], return_scale=True)
+        assert werr(g[idx], ref, S) < W_TOL, j["name"]
+    alone = ctx.batch_eval([heavy[2]], graph=False)[0]
+    assert ctx.last_launches() == (2, "persistent-batch")
+    for a_, b_ in zip(alone, outs[3]):
+        np.testing.assert_array_equal(a_, b_)

@@ -163,8 +163,8 @@ def test_invalid_requests_are_refused_at_submit():
             srv.submit_w(1, 1000, 64, fld, [0.1], [0.0], [0.5], [1.0], group=128)
         with pytest.raises(wltube.WlError):        # T <= 0
             srv.submit_w(1, 256, 64, fld, [0.1], [0.0], [0.0], [1.0])
-        with pytest.raises(wltube.WlError):        # profile outside the batch kernel
-            srv.submit_w(1, 256, 64, wltube.field("periodic", nint=4), [0.1], [0.0], [0.5],
+        with pytest.raises(wltube.WlError):        # odd interval count
+            srv.submit_w(1, 256, 64, wltube.field("periodic", nint=5), [0.1], [0.0], [0.5],
                          [1.0])
         with pytest.raises(wltube.WlError):        # T grid not log-spaced
             srv.submit_leff(1, 256, 64, fld, [0.0], [0.1, 0.2, 0.4, 0.5], [1.0], nbins=2)
@@ -219,3 +219,45 @@ def test_many_concurrent_requests_equal_alone():
             assert np.array_equal(g, g1) and np.array_equal(m, m1) and np.array_equal(s, s1)
         for h in handles.values():
             ctx.release(h)
+
+
+def test_served_heavy_profiles_equal_alone():
+    """Periodic, spline and fixflux requests (not in the persistent kernel:
+    chunk ranges of their own sweep per quantum) beside a smooth one: each
+    result equals the request alone in a batch, bit for bit, and L_eff of a
+    spline request equals wl_tint."""
+    import wltube
+
+    rng = np.random.default_rng(23)
+    specs = [("periodic", 1, 0, 1.0, 40), ("spline", 0, 0, 2.0, 150), ("fixflux", 0, 0, 2.0, 20),
+             ("fixflux", 1, 1, 2.0, 9), ("smooth", 1, 0, 1.0, 300)]
+    reqs = []
+    for prof, fe, ffv, a, n in specs:
+        cx, cy, T = f32_exact(rng.uniform(0, 2 * a, n), rng.uniform(-0.2, 0.2, n),
+                              np.exp(rng.uniform(np.log(0.02), np.log(2.0), n)))
+        fld = wltube.field(prof, fermion=fe, nint=8, lambda2=0.5, tubedist=a, ff_variant=ffv)
+        reqs.append((prof, fld, cx, cy, T))
+    rho, Tg, F = np.linspace(0.0, 2.0, 3), np.geomspace(1e-2, 2.0, 5), [1.0]
+    spl = wltube.field("spline", fermion=0, nint=8, lambda2=0.5, tubedist=2.0)
+    # 64 loop chunks per request (16384 points per tile, the batch default)
+    # and one persistent CTA per SM: ~500 tiles, several quanta, so the heavy
+    # requests run as sweeps over chunk ranges that start past chunk 0
+    with wltube.Server(0, quantum_ms=0.5, ctas_per_sm=1) as srv:
+        tickets = [srv.submit_w(31, 8192, 128, fld, cx, cy, T, [0.5, 1.0], group=128,
+                                want_groups=True) for _, fld, cx, cy, T in reqs]
+        tl = srv.submit_leff(31, 8192, 128, spl, rho, Tg, F, group=128, nbins=2)
+        served = [done(srv, t) for t in tickets]
+        le, er = done(srv, tl)
+        st = srv.stats()
+    assert st["completed"] == len(reqs) + 1 and st["failed"] == 0
+    assert st["launches"] >= 3
+    with wltube.Context(0) as ctx:
+        h = ctx.generate(31, 8192, 128)
+        for (prof, fld, cx, cy, T), (g, m, s) in zip(reqs, served):
+            job = {"handle": h, "field": fld, "cx": cx, "cy": cy, "T": T, "F": [0.5, 1.0],
+                   "group": 128}
+            (g1, m1, s1), = ctx.batch_eval([job], graph=False)
+            assert np.array_equal(g, g1) and np.array_equal(m, m1), prof
+        le1, er1, _ = ctx.tint(h, spl, rho, Tg, F, group=128, nbins=2)
+        ctx.release(h)
+    assert np.all(np.abs(le - le1) <= 1e-7 * np.abs(le1) + 1e-4 * er1)

@@ -386,6 +386,7 @@ struct BatchPlan {
   size_t perm_total = 0;  // lattice jobs' instance orders
   std::vector<wl::SweepArgs> jobs;
   std::vector<wl::BatchTile> tiles;
+  std::vector<int> side;  // heavy-profile jobs: their own sweep launch each
   std::vector<wl::ReduceJob> rjobs;
   std::vector<float> inst;
   size_t part_total = 0, out_total = 0;
@@ -471,6 +472,10 @@ int batch_plan(wl_ctx *ctx, int njobs, const wl_job *jobs, int points, BatchPlan
     rj.first = P->flat_total;
     rj.out_group = (double *)(uintptr_t)(out_off[i]);
     P->flat_total += n * J.nF;
+    if (!wl::batch_in_kernel(kprofs[i])) {
+      P->side.push_back(i);
+      continue;
+    }
     const int per_tile = wl::sweep_tile_instances(kprofs[i], J.field.nint);
     const int tiles_x = (n + per_tile - 1) / per_tile;
     const int cost = lcs[i] * e.ppl * (per_tile / wl::kSweepThreads);
@@ -489,7 +494,7 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
   BatchPlan P;
   int r = batch_plan(ctx, njobs, jobs, points, &P);
   if (r) return r;
-  if (P.tiles.empty()) return fail(ctx, WL_ERR_INVALID, "empty batch");
+  if (P.tiles.empty() && P.side.empty()) return fail(ctx, WL_ERR_INVALID, "empty batch");
   const size_t jobs_bytes = sizeof(wl::SweepArgs) * njobs;
   const size_t tiles_bytes = sizeof(wl::BatchTile) * P.tiles.size();
   const size_t rj_bytes = sizeof(wl::ReduceJob) * njobs;
@@ -551,13 +556,23 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
   int grid = per_sm * ctx->num_sms;
   if (grid > B.ntiles) grid = B.ntiles;
   const wl::ReduceJob *rjd = (const wl::ReduceJob *)(meta + off_rj);
+  // kernels per run: the persistent kernel, the side sweeps, the reduction
+  const int launches = (B.ntiles > 0 ? 1 : 0) + (int)P.side.size() + 1;
 
   cudaEvent_t e0, e1;
   WL_CHECK(ctx, cudaEventCreate(&e0));
   WL_CHECK(ctx, cudaEventCreate(&e1));
   auto enqueue = [&]() -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(B.counter, 0, sizeof(int), ctx->stream);
-    if (e == cudaSuccess) e = wl::launch_batch(B, grid, ctx->stream);
+    cudaError_t e = cudaSuccess;
+    if (B.ntiles > 0) {
+      e = cudaMemsetAsync(B.counter, 0, sizeof(int), ctx->stream);
+      if (e == cudaSuccess) e = wl::launch_batch(B, grid, ctx->stream);
+    }
+    for (int i : P.side) {  // heavy profiles: their own sweep, same partial layout
+      if (e != cudaSuccess) break;
+      const wl::SweepArgs &a = P.jobs[i];
+      e = wl::launch_sweep(a.kprof, a.fermion != 0, a.nint, a, ctx->stream);
+    }
     if (e == cudaSuccess) e = wl::launch_batch_reduce(rjd, njobs, P.flat_total, ctx->stream);
     return e;
   };
@@ -591,7 +606,7 @@ int batch_run(wl_ctx *ctx, int njobs, const wl_job *jobs, int flags, int points,
   ctx->last_batch_ms = ms;
   ctx->last_batch_tiles = B.ntiles;
   ctx->last_batch_grid = grid;
-  ctx->last_launches = 2;
+  ctx->last_launches = launches;
   ctx->last_kind = "persistent-batch";
   if ((r = check_status(ctx))) return r;
   if (!copy_out) return WL_OK;

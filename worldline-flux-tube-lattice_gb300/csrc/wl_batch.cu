@@ -225,9 +225,10 @@ cudaError_t launch_plain(int kprof, bool fermion, int nint, const LoopArgs &a, i
 
 bool batch_supports(int kprof, int nint) {
   (void)nint;
-  return kprof == kSmooth || kprof == kGaussian || kprof == kStep || kprof == kQuadratic ||
-         kprof == kLattice;
+  return kprof >= kStep && kprof <= kLattice;
 }
+
+bool batch_in_kernel(int kprof) { return light_profile(kprof) || kprof == kLattice; }
 
 bool plain_supports(int kprof) {
   return kprof == kSmooth || kprof == kGaussian || kprof == kStep || kprof == kQuadratic;

@@ -82,7 +82,12 @@ cudaError_t launch_batch(const BatchArgs &a, int grid, cudaStream_t s);
 cudaError_t launch_batch_reduce(const ReduceJob *jobs, int njobs, int total, cudaStream_t s);
 // largest number of batch-kernel CTAs resident per SM
 int batch_max_ctas_per_sm();
+// every profile batches; the heavy ones (periodic, spline, fixflux) are not
+// instantiated in the persistent kernel (their tiles would triple its
+// compilation time) and run as chunk-range launches of their own sweep
+// kernel beside it, with the same partial-sum layout
 bool batch_supports(int kprof, int nint);
+bool batch_in_kernel(int kprof);
 bool plain_supports(int kprof);
 
 // Loop-parallel sweep: one warp per (loop, instance), lanes over groups of

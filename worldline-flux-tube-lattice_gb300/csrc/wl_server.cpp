@@ -35,6 +35,7 @@
 
 #include "../../include/wlgpu.h"
 #include "wl_internal.h"
+#include "wl_spline.h"
 
 namespace wl {
 int rt_field(const wl_field *f, int *kprofile, FieldDev *d, std::string *err);
@@ -52,12 +53,29 @@ constexpr size_t kAlign = 256;
 
 size_t up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
-// relative device time of one tile-point of a profile (rate estimate only)
-double profile_weight(int kprof, int fermion) {
-  double w = 1.0;
-  if (kprof == wl::kGaussian) w = 1.6;
-  if (kprof == wl::kLattice) w = 8.0;
-  return fermion ? w * 1.15 : w;
+// Device time of one tile-point relative to the smooth profile at 4
+// intervals (the processor-sharing split and the rate estimate only): the
+// node count times the profile's cost relative to the smooth one at the same
+// interval count, measured on the GB300 through wl_eval (512 instances on
+// Nl 1024 x ppl 1024, scalar QED) at 4, 8 and 50 intervals and interpolated
+// linearly in nint between them (flat outside).
+double profile_weight(int kprof, int fermion, int nint) {
+  double r[3] = {1.0, 1.0, 1.0};  // at 4, 8, 50 intervals
+  switch (kprof) {
+    case wl::kGaussian: r[0] = 1.6; r[1] = 1.94; r[2] = 3.95; break;
+    case wl::kLattice: r[0] = r[1] = r[2] = 8.0; break;
+    case wl::kPeriodic: r[0] = r[1] = 44.6; r[2] = 127.8; break;
+    case wl::kSpline: r[0] = r[1] = 12.6; r[2] = 29.2; break;
+    case wl::kFixflux:
+    case wl::kFixfluxFF: r[0] = r[1] = 480.0; r[2] = 870.0; break;
+    default: break;
+  }
+  double w;
+  if (nint <= 4) w = r[0];
+  else if (nint <= 8) w = r[0] + (r[1] - r[0]) * (nint - 4) / 4.0;
+  else if (nint <= 50) w = r[1] + (r[2] - r[1]) * (nint - 8) / 42.0;
+  else w = r[2];
+  return (fermion ? w * 1.15 : w) * (nint + 1) / 5.0;
 }
 
 struct SrvEnsemble {
@@ -136,6 +154,8 @@ struct wl_server {
   double rate = 0.0;  // weighted tile work per ms of device time
   uint64_t use_clock = 0;
   std::map<size_t, std::vector<char *>> pin_cache;
+  // spline profile tables by (lambda^2, tube spacing), kept until destroy
+  std::map<std::pair<double, double>, std::pair<float *, float4 *>> splines;
 };
 
 namespace {
@@ -166,8 +186,7 @@ int check_request(wl_server *s, const wl_request *q, Req *R) {
   if (wl::rt_field(&q->field, &R->kprof, &R->fd, &e))
     return set_err(s, WL_ERR_INVALID, "%s", e.c_str());
   if (!wl::batch_supports(R->kprof, q->field.nint))
-    return set_err(s, WL_ERR_INVALID, "profile %d is not served (batch kernel profiles only)",
-                   q->field.profile);
+    return set_err(s, WL_ERR_INVALID, "profile %d is not served", q->field.profile);
   const int ng = q->Nl / q->group;
   if (q->kind == WL_REQ_W) {
     if (q->ninst < 1 || !q->cx || !q->cy || !q->T)
@@ -224,7 +243,7 @@ int check_request(wl_server *s, const wl_request *q, Req *R) {
   R->tiles_x = (n + per_tile - 1) / per_tile;
   R->ntiles = (long long)R->n_chunks * R->tiles_x;
   R->tile_work = (double)R->lc * q->ppl * per_tile *
-                 profile_weight(R->kprof, q->field.fermion != 0);
+                 profile_weight(R->kprof, q->field.fermion != 0, q->field.nint);
   R->segments = (double)n * q->Nl * q->ppl;
   const size_t n_part = (size_t)R->n_chunks * nF * 3 * n;
   const size_t n_out = (size_t)n * nF * (ng + 2);
@@ -386,6 +405,28 @@ bool admit(wl_server *s) {
       s->in_use += (double)ne->bytes;
       E = ne.get();
       s->ens.push_back(std::move(ne));
+    }
+    if (R->kprof == wl::kSpline) {  // the profile's table, once per (lambda^2, a)
+      const auto key = std::make_pair(R->q.field.lambda2, R->q.field.tubedist);
+      auto it = s->splines.find(key);
+      if (it == s->splines.end()) {
+        const int nk = wl::kSplineKnots;
+        std::vector<float> rho2(nk), coef(4 * (size_t)nk);
+        float *dr = nullptr;
+        float4 *dc = nullptr;
+        // the field was validated at submit, so the table is well defined
+        wl::spline_table(R->q.field.lambda2, R->q.field.tubedist, nk, rho2.data(), coef.data());
+        ck(cudaMallocAsync((void **)&dr, sizeof(float) * nk, s->cs), "spline table");
+        ck(cudaMallocAsync((void **)&dc, sizeof(float4) * nk, s->cs), "spline table");
+        // pageable sources: staged before the calls return
+        ck(cudaMemcpyAsync(dr, rho2.data(), sizeof(float) * nk, cudaMemcpyHostToDevice, s->cs),
+           "spline upload");
+        ck(cudaMemcpyAsync(dc, coef.data(), sizeof(float4) * nk, cudaMemcpyHostToDevice, s->cs),
+           "spline upload");
+        it = s->splines.emplace(key, std::make_pair(dr, dc)).first;
+      }
+      R->fd.sp_rho2 = it->second.first;
+      R->fd.sp_coef = it->second.second;
     }
     if (R->kprof == wl::kLattice && !E->bbox) {
       const size_t bb = (size_t)E->Nl * sizeof(float4);
@@ -560,10 +601,28 @@ void launch_quantum(wl_server *s, int k) {
   }
   double work = 0.0;
   int n = 0;
+  long long side_tiles = 0;
   std::vector<Req *> closing;
+  struct Side {  // a heavy-profile request's loop chunks [c0, c0 + nc)
+    Req *R;
+    int c0, nc;
+  };
+  std::vector<Side> side;
   wl::BatchTile *h = s->h_tiles[k];
   for (size_t i = 0; i < m && n < kMaxQuantumTiles; ++i) {
     Req *R = act[i];
+    if (!wl::batch_in_kernel(R->kprof)) {
+      // not in the persistent kernel: whole loop chunks, as a sweep launch
+      // over them (next_tile stays a multiple of tiles_x)
+      const long long tx = R->tiles_x;
+      const long long t = std::min(left(i), (take[i] + tx - 1) / tx * tx);
+      side.push_back({R, (int)(R->next_tile / tx), (int)(t / tx)});
+      R->next_tile += t;
+      side_tiles += t;
+      work += (double)t * R->tile_work;
+      if (R->next_tile >= R->ntiles) closing.push_back(R);
+      continue;
+    }
     const int cost = R->lc * R->q.ppl *
                      (wl::sweep_tile_instances(R->kprof, R->q.field.nint) / wl::kSweepThreads);
     for (long long c = 0; c < take[i] && n < kMaxQuantumTiles; ++c) {
@@ -577,21 +636,33 @@ void launch_quantum(wl_server *s, int k) {
   std::stable_sort(h, h + n, [](const wl::BatchTile &x, const wl::BatchTile &y) {
     return x.cost > y.cost;
   });
-  ck(cudaMemcpyAsync(s->d_tiles[k], h, sizeof(wl::BatchTile) * n, cudaMemcpyHostToDevice, st),
-     "tile upload");
-  ck(cudaMemsetAsync(s->d_counter + k, 0, sizeof(int), st), "counter reset");
-  wl::BatchArgs B;
-  B.jobs = s->d_slots;
-  B.tiles = s->d_tiles[k];
-  B.ntiles = n;
-  B.counter = s->d_counter + k;
-  const int grid = std::min(s->grid_max, n);
+  if (n > 0) {
+    ck(cudaMemcpyAsync(s->d_tiles[k], h, sizeof(wl::BatchTile) * n, cudaMemcpyHostToDevice, st),
+       "tile upload");
+    ck(cudaMemsetAsync(s->d_counter + k, 0, sizeof(int), st), "counter reset");
+  }
   ck(cudaEventRecord(s->ev_start[k], st), "event");
-  ck(wl::launch_batch(B, grid, st), "batch launch");
+  if (n > 0) {
+    wl::BatchArgs B;
+    B.jobs = s->d_slots;
+    B.tiles = s->d_tiles[k];
+    B.ntiles = n;
+    B.counter = s->d_counter + k;
+    ck(wl::launch_batch(B, std::min(s->grid_max, n), st), "batch launch");
+  }
+  for (const Side &x : side) {  // the request's own sweep over its chunk range
+    const Req *R = x.R;
+    wl::SweepArgs a = R->args;
+    a.loops += (size_t)x.c0 * R->lc * R->q.ppl;
+    a.partial += (size_t)x.c0 * R->q.nF * 3 * R->ninst;
+    a.n_chunks = x.nc;
+    ck(wl::launch_sweep(R->kprof, R->q.field.fermion != 0, R->q.field.nint, a, st),
+       "sweep launch");
+  }
   ck(cudaEventRecord(s->ev_stop[k], st), "event");
   s->busy[k] = true;
   s->busy_work[k] = work;
-  s->busy_tiles[k] = n;
+  s->busy_tiles[k] = n + (int)std::min<long long>(side_tiles, 1 << 30);
   if (!closing.empty()) {
     // earlier tiles of these requests may be in the other stream's launch
     ck(cudaStreamWaitEvent(st, s->ev_stop[k ^ 1], 0), "wait other stream");
@@ -944,6 +1015,10 @@ int wl_server_destroy(wl_server *srv) {
   }
   for (auto &kv : srv->pin_cache)
     for (char *p : kv.second) cudaFreeHost(p);
+  for (auto &kv : srv->splines) {
+    cudaFree(kv.second.first);
+    cudaFree(kv.second.second);
+  }
   if (srv->adm_ev) cudaEventDestroy(srv->adm_ev);
   if (srv->d_counter) cudaFree(srv->d_counter);
   if (srv->d_slots) cudaFree(srv->d_slots);
