@@ -482,12 +482,15 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
       return cudaGetLastError();
     }
   }
-#ifndef WL_SMOOTH50_PAIRS
-#define WL_SMOOTH50_PAIRS 1
+#ifndef WL_PAIRS50
+#define WL_PAIRS50 1
 #endif
-  if constexpr (P == kSmooth && WL_SMOOTH50_PAIRS) {
-    if (nint == 50) {  // the reference's interval count: packed pairs, a share
-                       // of the reciprocals on the FP32 pipe
+  if constexpr ((P == kSmooth || P == kStep || P == kQuadratic || P == kGaussian) && WL_PAIRS50) {
+    if (nint == 50) {  // the reference's interval count: packed pairs (smooth:
+                       // a share of the reciprocals on the FP32 pipe); measured
+                       // over one instance per thread: smooth +3 % / +7 %
+                       // (scalar / spinor), Gaussian +56 % / +54 %, step
+                       // +4 % / +31 %, quadratic +35 % / +24 %
       if (fermion)
         sweep2_kernel<P, true, 50><<<grid2, kSweepThreads, smem, s>>>(a);
       else
@@ -495,10 +498,10 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
       return cudaGetLastError();
     }
   }
-  // one instance per thread: other interval counts (50 unrolled for the
-  // other light profiles; others at run time -- a run-time-interval pair
-  // kernel measured 26 % slower than the unrolled 50), the lattice at 4 too,
-  // and the heavy profiles
+  // one instance per thread: other interval counts at run time (a
+  // run-time-interval pair kernel measured 26 % slower than the unrolled
+  // scalar 50), the lattice at 4 too, and the heavy profiles; the scalar 50
+  // serves the loop-parallel kernel
 #define WL_SWEEP_CASE(FE, NI)                                                      \
   if (fermion == FE && (NI == 0 || nint == NI)) {                                  \
     sweep_kernel<P, FE, NI><<<grid, kSweepThreads, smem, s>>>(a);                  \
