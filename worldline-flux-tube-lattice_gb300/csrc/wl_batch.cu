@@ -15,13 +15,13 @@ namespace wl {
 namespace {
 
 // One tile of a job: packed pairs (256 instances) for the light profiles at
-// 4 intervals -- as the single-job sweep, so such a job's results match it bit
-// for bit -- one instance per thread otherwise (sweep_tile_instances).
+// 4 and 50 intervals -- as the single-job sweep, so such a job's results match
+// it bit for bit -- one instance per thread otherwise (sweep_tile_instances).
 template <bool FERM, int NINT>
 __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, int chunk,
                                          const SweepShared &S, double (*sacc2)[kPairTile],
                                          int &consumed) {
-  if constexpr (NINT != 4) {
+  if constexpr (NINT == 0) {
     switch (kprof) {
       case kSmooth: sweep_tile<kSmooth, FERM, NINT>(A, tx, chunk, S, consumed); break;
       case kGaussian: sweep_tile<kGaussian, FERM, NINT>(A, tx, chunk, S, consumed); break;
@@ -48,7 +48,9 @@ __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, 
         sweep_tile2<kQuadratic, FERM, NINT>(A, tx, chunk, S.full_bar, sacc2, S.bad, S.ring,
                                             consumed);
         break;
-      case kLattice: sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed); break;
+      case kLattice:
+        if constexpr (NINT == 4) sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed);
+        break;
       default: break;
     }
   }
@@ -92,14 +94,21 @@ __global__ void __launch_bounds__(kSweepThreads, kBatchMinBlocks)
     }
     __syncthreads();
     const int tx = cur[2], chunk = cur[3];
+    // 4 and 50 intervals (the reference's): unrolled, pairs for the light
+    // profiles; any other count at run time
+    const bool n50 = job.nint == 50 && light_profile(job.kprof);
     if (job.fermion) {
       if (job.nint == 4)
         run_tile<true, 4>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+      else if (n50)
+        run_tile<true, 50>(job.kprof, job, tx, chunk, S, sacc2, consumed);
       else
         run_tile<true, 0>(job.kprof, job, tx, chunk, S, sacc2, consumed);
     } else {
       if (job.nint == 4)
         run_tile<false, 4>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+      else if (n50)
+        run_tile<false, 50>(job.kprof, job, tx, chunk, S, sacc2, consumed);
       else
         run_tile<false, 0>(job.kprof, job, tx, chunk, S, sacc2, consumed);
     }
