@@ -32,7 +32,9 @@ def setup():
              ("gaussian", 1, 4, 0.5, (128, 256), 37, [2.0]),
              ("smooth", 0, 8, 2.0, (256, 512), 140, [0.1, 0.3, 1.0]),
              ("step", 0, 4, 3.0, (64, 256), 9, [1.0]),
-             ("quadratic", 1, 4, 1.5, (128, 256), 300, [0.7])]
+             ("quadratic", 1, 4, 1.5, (128, 256), 300, [0.7]),
+             ("smooth", 0, 50, 0.5, (64, 256), 270, [1.0]),      # pair tiles at 50
+             ("gaussian", 1, 50, 1.0, (128, 256), 30, [0.4, 1.2])]
     jobs = []
     for prof, fe, nint, l2, key, n, F in specs:
         cx, cy, T = f32_exact(rng.uniform(0, 2.5, n), rng.uniform(-0.2, 0.2, n),
@@ -62,7 +64,7 @@ def test_batch_matches_oracle_and_single_jobs(setup):
 def test_batch_results_do_not_depend_on_the_mix(setup):
     ctx, jobs, _ = setup
     mixed = ctx.batch_eval(jobs, graph=False)
-    for k in (0, 3):
+    for k in (0, 3, 5):
         alone = ctx.batch_eval([jobs[k]], graph=True)[0]
         for a, b in zip(alone, mixed[k]):
             np.testing.assert_array_equal(a, b)

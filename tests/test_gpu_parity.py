@@ -123,6 +123,9 @@ def _instances(n, rho_max, Tlo, Thi, seed):
     ("smooth", 0, 4, 1.0, W_TOL), ("smooth", 1, 4, 1.0, W_TOL), ("smooth", 1, 50, 1.0, W_TOL),
     ("gaussian", 1, 4, 1.0, W_TOL), ("gaussian", 0, 50, 0.25, W_TOL),
     ("quadratic", 1, 8, 1.0, W_TOL), ("step", 0, 4, 2.0, W_TOL),
+    ("smooth", 0, 50, 0.01, W_TOL), ("gaussian", 1, 50, 1.0, W_TOL),
+    ("quadratic", 0, 50, 1.0, W_TOL), ("quadratic", 1, 50, 1.0, W_TOL),
+    ("step", 0, 50, 2.0, W_TOL),
     # the step profile's f' jumps from 1/lambda^2 to 0 at rho^2 = lambda^2: a
     # Simpson node within FP32 rounding of the edge lands on either side in the
     # FP32 kernel and the FP64 oracle, which moves that loop's spin exponent by
