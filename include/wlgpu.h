@@ -188,6 +188,16 @@ int wl_eval_device(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
  * lane operations per second over the whole device (about 0.1 s of work). */
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s);
 
+/* Self-test of the device's bounded waits (every shared-memory stage copy
+ * is awaited by a bounded mbarrier wait that, when it gives up, sets the
+ * launch's status so that the call returns WL_ERR_TIMEOUT and the context
+ * stays usable).  One CTA waits, max_tries polls (1 .. 2^22; the sweeps use
+ * 2^22) at most, on an mbarrier that gets its arrival (arrive = 1: returns
+ * WL_OK) or never does (arrive = 0: the wait gives up and the call returns
+ * WL_ERR_TIMEOUT).  No copy is issued.  *device_ms (may be NULL) receives the
+ * kernel's time, i.e. how long max_tries polls take. */
+int wl_selftest_wait(wl_ctx *ctx, int arrive, int max_tries, double *device_ms);
+
 /* The spline profile's table for lambda^2 and the tube spacing (host only, no
  * device needed): knots rho2[n] (rho_i^2 as float, rho_i = 20 i/n) and the
  * spline coefficients coef4[n][4] = (f, b, c, d) of f + b d + c d^2 + d d^3,

@@ -163,3 +163,26 @@ def test_nan_loop_poisons_only_its_group(ctx):
         np.testing.assert_array_equal(g2[:, 0, [0, 1, 3]], g[:, 0, [0, 1, 3]])
     finally:
         ctx.release(h)
+
+
+def test_bounded_wait_gives_up_with_a_status(ctx):
+    """The bounded mbarrier wait that guards every staged copy, on a barrier
+    nothing arrives at: the kernel gives up, the call returns the timeout
+    status, and the context stays usable (no fault, no hang)."""
+    import wltube
+
+    ctx.selftest_wait(True)
+    for tries in (1, 16, 64):
+        with pytest.raises(wltube.WlError) as e:
+            ctx.selftest_wait(False, tries)
+        assert e.value.status == -4
+        assert ctx.last_launches() == (1, "wait-selftest")
+    ctx.selftest_wait(True, 64)
+    loops = O.vloops(36, 128, 64)
+    cx, cy, T = instances(40, 5)
+    h = ctx.upload(loops)
+    try:
+        g, _, _ = ctx.eval(h, wltube.field("smooth", fermion=0, nint=4), cx, cy, T, [1.0])
+    finally:
+        ctx.release(h)
+    assert np.all(np.isfinite(g))

@@ -1019,6 +1019,30 @@ int wl_spline_table(double lambda2, double tubedist, int n, float *rho2, float *
   return wl::spline_table(lambda2, tubedist, n, rho2, coef4) ? WL_ERR_INVALID : WL_OK;
 }
 
+int wl_selftest_wait(wl_ctx *ctx, int arrive, int max_tries, double *device_ms) {
+  if (!ctx || max_tries < 1 || max_tries > (1 << 22))
+    return fail(ctx, WL_ERR_INVALID, "max_tries must be in [1, 2^22]");
+  int r = set_device(ctx);
+  if (r) return r;
+  cudaEvent_t e0, e1;
+  WL_CHECK(ctx, cudaEventCreate(&e0));
+  WL_CHECK(ctx, cudaEventCreate(&e1));
+  WL_CHECK(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(int), ctx->stream));
+  WL_CHECK(ctx, cudaEventRecord(e0, ctx->stream));
+  WL_CHECK(ctx, wl::launch_wait_selftest(ctx->status.p, (uint32_t)max_tries, arrive ? 1 : 0,
+                                         ctx->stream));
+  WL_CHECK(ctx, cudaEventRecord(e1, ctx->stream));
+  WL_CHECK(ctx, cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (device_ms) *device_ms = ms;
+  ctx->last_launches = 1;
+  ctx->last_kind = "wait-selftest";
+  return check_status(ctx);
+}
+
 int wl_peak_probe(wl_ctx *ctx, int kind, double *ops_per_s) {
   if (!ctx || !ops_per_s || kind < 0 || kind > 2) return fail(ctx, WL_ERR_INVALID, "bad probe");
   int r = set_device(ctx);

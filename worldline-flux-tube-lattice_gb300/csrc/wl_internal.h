@@ -137,6 +137,8 @@ cudaError_t launch_instance_setup(const double *cx, const double *cy, const doub
 
 // pipe throughput probes: kind 0 FP32 FMA chains, 1 MUFU rcp chains;
 // each thread performs iters * 8 operations
+// one CTA waiting (bounded) on an mbarrier that gets its arrival or not
+cudaError_t launch_wait_selftest(int *status, uint32_t max_tries, int arrive, cudaStream_t s);
 cudaError_t launch_peak_probe(int kind, int blocks, int threads, int iters, float *sink,
                               cudaStream_t s);
 

@@ -307,6 +307,30 @@ __global__ void peak_fma2_kernel(int iters, float *sink) {
   if (s == -1.0f) sink[blockIdx.x] = s;
 }
 
+// The bounded mbarrier wait that guards every staged copy, on its own: one
+// CTA initialises a barrier for one arrival and waits on its first phase
+// with max_tries polls.  With arrive = 1 thread 0 arrives (the phase
+// completes, nothing is written); with arrive = 0 nothing arrives, the wait
+// gives up and the status word receives kDevTimeout.  No copy is issued, so
+// nothing is in flight when the CTA exits.
+__global__ void wait_selftest_kernel(int *status, uint32_t max_tries, int arrive) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && arrive) mbar_arrive_expect_tx(&bar, 0);
+  const bool ok = mbar_wait_bounded(&bar, 0, max_tries);
+  __syncthreads();
+  if (threadIdx.x == 0 && !ok) atomicExch(status, kDevTimeout);
+}
+
+cudaError_t launch_wait_selftest(int *status, uint32_t max_tries, int arrive, cudaStream_t s) {
+  wait_selftest_kernel<<<1, 32, 0, s>>>(status, max_tries, arrive);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_peak_probe(int kind, int blocks, int threads, int iters, float *sink,
                               cudaStream_t s) {
   if (kind == 0)

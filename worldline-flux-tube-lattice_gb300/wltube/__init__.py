@@ -148,6 +148,7 @@ def lib():
         L.wl_tint.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_int, dp, C.c_int, dp, C.c_int, dp,
                               C.c_int, C.c_int, dp, dp, dp]
         L.wl_peak_probe.argtypes = [vp, C.c_int, dp]
+        L.wl_selftest_wait.argtypes = [vp, C.c_int, C.c_int, dp]
         L.wl_spline_table.argtypes = [C.c_double, C.c_double, C.c_int, fp, fp]
         L.wl_effective_action.argtypes = [vp, C.c_int, C.POINTER(Field), C.c_double, C.c_int,
                                           C.c_int, dp, C.c_int, C.c_int, dp, dp, dp, dp]
@@ -420,6 +421,15 @@ class Context:
         v = C.c_double()
         self._check(lib().wl_peak_probe(self._h, kind, C.byref(v)))
         return v.value
+
+    def selftest_wait(self, arrive: bool, max_tries: int = 64) -> float:
+        """The device's bounded mbarrier wait on a barrier that gets its
+        arrival (returns the kernel's ms) or never does (raises WlError,
+        status -4)."""
+        ms = C.c_double()
+        self._check(lib().wl_selftest_wait(self._h, int(bool(arrive)), int(max_tries),
+                                           C.byref(ms)))
+        return ms.value
 
     def stream(self) -> int:
         """The context's cudaStream_t as an integer."""
