@@ -515,6 +515,62 @@ def run_lattice(args):
     ctx.close()
 
 
+def effact_legacy(ctx, h, Nl, ppl, l2, F, nrho, panels):
+    """The same effective action through the reference's own caller chain,
+    relinked against this library and otherwise unchanged: for every radial
+    node of EAction's rule (EffAct.c:258-306) rhogrand's integrateT(40, p)
+    (EffAct.c:15-40) -> Tfunc -> EV() with a struct Wparams of device buffers
+    (EffAct.c:368-413), EV at the reference's 50 intervals; then the same
+    radial sum.  Returns its time, action and EV() calls.  The Leffvsrho
+    lines integrateT prints go to /dev/null."""
+    import ctypes as C
+
+    import torch
+    import wltube
+
+    wltube.legacy_configure("smooth", nint=50)
+    scal_d = torch.zeros(Nl * 4, device="cuda")
+    ferm_d = torch.zeros(Nl * 4, device="cuda")
+    scal_h = np.zeros((Nl, 4), dtype=np.float32)
+    ferm_h = np.zeros((Nl, 4), dtype=np.float32)
+    p = wltube.Wparams()
+    p.Nl, p.Nppl, p.F, p.l2, p.fermion, p.ng = Nl, ppl, F, l2, 0, Nl // 128
+    p.worldlines = ctx.device_pointer(h)
+    p.Wsscal_d, p.Wsferm_d = scal_d.data_ptr(), ferm_d.data_ptr()
+    p.Wsscal_h, p.Wsferm_h = scal_h.ctypes.data, ferm_h.ctypes.data
+    # EAction's radial nodes rho = (1 - t)/t and weights (the reference's rule)
+    hh = 1.0 / nrho
+    wt = np.zeros(2 * nrho + 1)
+    for i in range(nrho):
+        wt[2 * i + 2] += 2 * hh / 6
+        wt[2 * i + 1] += 4 * hh / 6
+    t = 0.5 * hh * np.arange(1, 2 * nrho + 1)
+    rho, w = (1 - t) / t, wt[1:] / t ** 2
+    libc = C.CDLL(None)
+    sys.stdout.flush()
+    saved, null = os.dup(1), os.open(os.devnull, os.O_WRONLY)
+    os.dup2(null, 1)
+    try:
+        t0 = time.perf_counter()
+        I = []
+        for r in rho:
+            p.xcm.x, p.xcm.y = float(r), 0.0
+            I.append(wltube.integrateT(panels, p))
+        sec = time.perf_counter() - t0
+        libc.fflush(None)
+    finally:
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(null)
+        wltube.legacy_configure("smooth")
+    I = np.array(I)
+    groups = -1.0 / (2 * np.pi) * np.einsum("r,r,rg->g", w, rho, np.where(np.isinf(I), 0.0, I))
+    return {"value": sec, "unit": "s", "effective_action": float(groups.mean()),
+            "standard_error": float(groups.std(ddof=1) / np.sqrt(len(groups))),
+            "path": "integrateT -> Tfunc -> EV (libwlhost.so, libwlgpu.so), one call per "
+                    "radial node"}
+
+
 def run_effact(args):
     """The reference driver's own run (EffAct.c:300-520, its main): the
     effective action of a smooth tube (F = 1, lambda = lmin = 0.1 a, a = 1)
@@ -537,12 +593,14 @@ def run_effact(args):
     ninst = 2 * 20 * (2 * 40 - 1)  # radial nodes x proper-time nodes
     segs = ninst * Nl * ppl
     sec = float(np.median(times))
+    legacy = effact_legacy(ctx, h, Nl, ppl, 0.01, 1.0, 20, 40)
     print(json.dumps({
         "metric": "effective action per call (the reference driver's configuration)",
         "value": sec, "unit": "s", "higher_is_better": False,
         "segments_per_call": segs, "segments_per_s": segs / sec,
         "instances": ninst, "effective_action": out[0], "standard_error": out[1],
         "classical_action": out[2], "steps": len(times),
+        "legacy_drop_in": legacy,
         "config": {"workload": "EffAct main: smooth, scalar, F=1, lambda^2=0.01, Nl=5120 x "
                                "Nppl=1024 (seed 2), 40 groups, rho rule 20 panels, integrateT "
                                "rule 40 panels, 50 Simpson intervals"}}))

@@ -168,3 +168,48 @@ def test_effective_action_with_the_reference_T_rule(prof, fermion):
     # far inside the Monte Carlo error
     assert abs(act - ref_g.mean()) <= 0.05 * ref_se + 1e-12
     np.testing.assert_allclose(groups, ref_g, rtol=0, atol=0.05 * ref_se + 1e-12)
+
+
+def test_legacy_integrateT_through_the_host_layer(capfd):
+    """The reference's own caller chain, unchanged: integrateT (Tint.c:100-175)
+    -> Tfunc (Integrand.c:195-316) -> EV (intEV.cu:111-148) through
+    libwlhost.so and libwlgpu.so with a struct Wparams of device buffers, as
+    EffAct.c:368-413 sets them up; per-group integrals against the oracle's
+    integrateT, and the Leffvsrho line the reference prints."""
+    import ctypes
+
+    torch = pytest.importorskip("torch")
+    import wltube
+
+    loops = O.vloops(12, 512, 128)
+    Nl, ppl = loops.shape[:2]
+    rho, F, l2 = 0.7, 1.0, 0.5
+    wltube.legacy_configure("smooth", nint=4)
+    try:
+        dev = torch.from_numpy(loops.reshape(-1)).cuda()
+        scal_d = torch.zeros(Nl * 4, device="cuda")
+        ferm_d = torch.zeros(Nl * 4, device="cuda")
+        scal_h = np.zeros((Nl, 4), dtype=np.float32)
+        ferm_h = np.zeros((Nl, 4), dtype=np.float32)
+        for fermion in (0, 1):
+            p = wltube.Wparams()
+            p.Nl, p.Nppl, p.F, p.l2, p.fermion, p.ng = Nl, ppl, F, l2, fermion, Nl // 128
+            p.xcm.x, p.xcm.y = rho, 0.0
+            p.worldlines = dev.data_ptr()
+            p.Wsscal_d, p.Wsferm_d = scal_d.data_ptr(), ferm_d.data_ptr()
+            p.Wsscal_h, p.Wsferm_h = scal_h.ctypes.data, ferm_h.ctypes.data
+            got = wltube.integrateT(40, p)
+            ref, _, _ = O.integrateT(loops, 40, rho, 0.0, F,
+                                  O.field("smooth", fermion=fermion, nint=4, lambda2=l2))
+            se = ref.std(ddof=1) / np.sqrt(len(ref))
+            # EV evaluates W at T' = float(sqrt(T))^2, the oracle at T
+            np.testing.assert_allclose(got, ref, rtol=0, atol=0.05 * se + 1e-12)
+            ctypes.CDLL(None).fflush(None)  # the C library's stdout buffer
+            out = capfd.readouterr().out.strip().splitlines()
+            tag = [line for line in out if line.startswith("Leffvsrho:")]
+            assert len(tag) == 1
+            x, leff, err = map(float, tag[0].split()[1:])
+            norm = 4 * np.pi if fermion else -2 * np.pi
+            assert abs(x - rho) < 1e-6 and np.isclose(leff, got.mean() / norm, rtol=1e-5)
+    finally:
+        wltube.legacy_configure("smooth")

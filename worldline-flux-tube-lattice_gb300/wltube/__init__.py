@@ -189,8 +189,38 @@ def host_lib():
         H.wlh_write_ensemble.argtypes = [C.c_char_p, vp, C.c_int, C.c_int, C.c_uint64]
         H.wlh_ensemble_file_info.argtypes = [C.c_char_p, ip, ip, C.POINTER(C.c_uint64)]
         H.wlh_read_ensemble.argtypes = [C.c_char_p, vp, C.c_int, C.c_int]
+        H.integrateT.argtypes = [C.c_int, vp]
+        H.integrateT.restype = C.POINTER(C.c_double)
+        H.Tfunc.argtypes = [C.c_double, vp, ip]
+        H.Tfunc.restype = C.POINTER(C.c_double)
         _host = H
     return _host
+
+
+_libc = None
+
+
+def _free(ptr):
+    """free() of the C library for the host layer's malloc'd results."""
+    global _libc
+    if _libc is None:
+        _libc = C.CDLL(None)
+        _libc.free.argtypes = [C.c_void_p]
+    _libc.free(C.cast(ptr, C.c_void_p))
+
+
+def integrateT(n: int, params: "Wparams") -> np.ndarray:
+    """The reference's integrateT(n, p) (Tint.c:100-175) through the C host
+    layer: the proper-time integral of every loop group, Simpson with n
+    panels in t, T = (1 - t)/t, each Tfunc evaluated through EV() on the
+    device.  Like the reference it prints the Leffvsrho line to stdout."""
+    ptr = host_lib().integrateT(int(n), C.cast(C.pointer(params), C.c_void_p))
+    if not ptr:
+        raise WlError(-1, "integrateT")
+    try:
+        return np.ctypeslib.as_array(ptr, shape=(params.ng,)).copy()
+    finally:
+        _free(ptr)
 
 
 def save_ensemble(path: str, loops: np.ndarray, seed: int = 0):
@@ -274,6 +304,13 @@ class Context:
         h = C.c_int()
         self._check(lib().wl_ensemble_generate(self._h, seed, first, Nl, ppl, C.byref(h)))
         return h.value
+
+    def device_pointer(self, handle: int) -> int:
+        """The ensemble's device address (float4 [Nl][ppl]), e.g. for the
+        worldlines field of a struct Wparams."""
+        ptr = C.c_void_p()
+        self._check(lib().wl_ensemble_info(self._h, handle, C.byref(ptr), None, None))
+        return ptr.value
 
     def download(self, handle: int) -> np.ndarray:
         Nl, ppl = C.c_int(), C.c_int()
