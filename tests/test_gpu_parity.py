@@ -230,6 +230,18 @@ def test_legacy_EV_matches_reference_golden(wl, gold):
         p.Wsferm_h = ferm_h.ctypes.data
         got = np.array([wl.EV(T, p, np.arange(g * 128, (g + 1) * 128)) for g in range(Nl // 128)])
         np.testing.assert_allclose(got, ref, rtol=W_TOL, err_msg=str(case))
+        # any other index list goes through the list kernel: a group in
+        # another order (FP64 sums in another order), and one loop repeated
+        # against its phases (Integrand.c:325-407's W factors, scalar QED)
+        rot = wl.EV(T, p, np.roll(np.arange(128, 256), 5))
+        assert abs(rot - got[1]) <= 1e-12 * max(abs(got[1]), 1.0)
+        if not fe:
+            sx, sy, sz = (float(v) for v in scal_h[7, :3])
+            one = (8 / 3 * np.cos(0.5 * sx + 0.25 * (sy + sz)) - 2 * np.cos(sx)
+                   + 1 / 3 * np.cos(0.5 * (sy + sz)))
+            # the phases in Wsscal_h are rounded to float: a few ulp of |phase|
+            tol = 20 * 2.0 ** -24 * max(abs(sx), abs(sy), abs(sz), 1.0)
+            assert abs(wl.EV(T, p, np.full(128, 7)) - one) <= tol, case
         # the reference's side effect: per-loop phases copied to Wsscal_h
         s64, f64 = O.loops_phases(loops, cx, 0.0, T, F, O.field(d, fermion=fe, lambda2=l2))
         assert np.abs(scal_h[:, :3] - s64).max() / np.abs(s64).max() < PHASE_TOL

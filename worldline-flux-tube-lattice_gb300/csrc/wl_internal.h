@@ -128,6 +128,10 @@ cudaError_t launch_group_reduce(const double *partial, int n_chunks, int chunks_
 // ninst = 1, nF = 1) and the Richardson combination; writes one double.
 cudaError_t launch_list_mean(const double *partial, const int *list, int n, double *out,
                              cudaStream_t s);
+// the same for the ngroups lists of n consecutive loops (g n .. g n + n - 1),
+// one double per group, each summed exactly as launch_list_mean sums it
+cudaError_t launch_group_list_means(const double *partial, int n, int ngroups, double *out,
+                                    cudaStream_t s);
 
 // device-resident instances (cx, cy, T) -> the sweep's float arrays
 // [cx | cy | rtT | tq_hi | tq_lo]; flags T <= 0 or non-finite values in *status

@@ -165,10 +165,11 @@ constexpr int kListThreads = 128;
 __global__ void __launch_bounds__(kListThreads)
     list_mean_kernel(const double *__restrict__ w, const int *__restrict__ list, int n,
                      double *__restrict__ out) {
+  // list == nullptr: block b takes the consecutive loops b n .. b n + n - 1
   __shared__ double red[3][kListThreads];
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   for (int i = threadIdx.x; i < n; i += kListThreads) {
-    const int l = list[i];
+    const int l = list ? list[i] : blockIdx.x * n + i;
     s0 += w[3 * (size_t)l];
     s1 += w[3 * (size_t)l + 1];
     s2 += w[3 * (size_t)l + 2];
@@ -184,14 +185,20 @@ __global__ void __launch_bounds__(kListThreads)
   }
   if (threadIdx.x == 0) {
     const double inv = 1.0 / (double)n;
-    out[0] = 1.0 + (8.0 / 3.0 * (red[0][0] * inv) - 2.0 * (red[1][0] * inv) +
-                    1.0 / 3.0 * (red[2][0] * inv));
+    out[blockIdx.x] = 1.0 + (8.0 / 3.0 * (red[0][0] * inv) - 2.0 * (red[1][0] * inv) +
+                             1.0 / 3.0 * (red[2][0] * inv));
   }
 }
 
 cudaError_t launch_list_mean(const double *partial, const int *list, int n, double *out,
                              cudaStream_t s) {
   list_mean_kernel<<<1, kListThreads, 0, s>>>(partial, list, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_group_list_means(const double *partial, int n, int ngroups, double *out,
+                                    cudaStream_t s) {
+  list_mean_kernel<<<ngroups, kListThreads, 0, s>>>(partial, nullptr, n, out);
   return cudaGetLastError();
 }
 
