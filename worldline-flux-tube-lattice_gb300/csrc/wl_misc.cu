@@ -13,6 +13,8 @@ cudaError_t launch_sweep_simple(int, bool, int, const SweepArgs *, const LoopArg
                                 cudaStream_t);
 cudaError_t launch_sweep_periodic(int, bool, int, const SweepArgs *, const LoopArgs *,
                                   cudaStream_t);
+cudaError_t launch_sweep_spline(int, bool, int, const SweepArgs *, const LoopArgs *,
+                                cudaStream_t);
 cudaError_t launch_sweep_fixflux(int, bool, int, const SweepArgs *, const LoopArgs *,
                                  cudaStream_t);
 cudaError_t launch_sweep_lattice(int, bool, int, const SweepArgs *, const LoopArgs *,
@@ -25,8 +27,8 @@ static cudaError_t dispatch(int profile, bool fermion, int nint, const SweepArgs
     case kStep:
     case kQuadratic:
     case kGaussian: return launch_sweep_simple(profile, fermion, nint, sa, la, s);
-    case kPeriodic:
-    case kSpline: return launch_sweep_periodic(profile, fermion, nint, sa, la, s);
+    case kPeriodic: return launch_sweep_periodic(profile, fermion, nint, sa, la, s);
+    case kSpline: return launch_sweep_spline(profile, fermion, nint, sa, la, s);
     case kFixflux:
     case kFixfluxFF: return launch_sweep_fixflux(profile, fermion, nint, sa, la, s);
     case kLattice: return launch_sweep_lattice(profile, fermion, nint, sa, la, s);

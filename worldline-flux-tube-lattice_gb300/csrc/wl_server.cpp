@@ -64,10 +64,10 @@ double profile_weight(int kprof, int fermion, int nint) {
   switch (kprof) {
     case wl::kGaussian: r[0] = 1.6; r[1] = 1.94; r[2] = 3.95; break;
     case wl::kLattice: r[0] = r[1] = r[2] = 8.0; break;
-    case wl::kPeriodic: r[0] = r[1] = 44.6; r[2] = 127.8; break;
+    case wl::kPeriodic: r[0] = r[1] = 30.4; r[2] = 70.8; break;
     case wl::kSpline: r[0] = r[1] = 12.6; r[2] = 29.2; break;
     case wl::kFixflux:
-    case wl::kFixfluxFF: r[0] = r[1] = 480.0; r[2] = 870.0; break;
+    case wl::kFixfluxFF: r[0] = r[1] = 180.0; r[2] = 400.0; break;
     default: break;
   }
   double w;

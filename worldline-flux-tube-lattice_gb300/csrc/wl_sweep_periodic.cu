@@ -1,4 +1,4 @@
-// wl_sweep_periodic.cu -- sweep kernel instantiations for profile(s): kPeriodic, kSpline
+// wl_sweep_periodic.cu -- sweep kernel instantiations for profile(s): kPeriodic
 // (split by profile so that the build compiles them in parallel).
 #include "wl_sweep.cuh"
 
@@ -10,9 +10,6 @@ cudaError_t launch_sweep_periodic(int profile, bool fermion, int nint, const Swe
     case kPeriodic:
       return sa ? sweep_dispatch<kPeriodic>(fermion, nint, *sa, s)
                 : loopwarp_dispatch<kPeriodic>(fermion, nint, *la, s);
-    case kSpline:
-      return sa ? sweep_dispatch<kSpline>(fermion, nint, *sa, s)
-                : loopwarp_dispatch<kSpline>(fermion, nint, *la, s);
     default:
       return cudaErrorInvalidValue;
   }
