@@ -1,6 +1,6 @@
 """Edge cases of the sweep through the C ABI: instance counts around the tile
 sizes (32 = loop-parallel threshold, 128 one-instance tiles, 256 pair
-tiles), loops whose point count is not a multiple of the 256-point staging
+tiles) at 4 and 50 intervals, loops whose point count is not a multiple of the 256-point staging
 chunk, the smallest loops (4 points), one group, the largest flux-value
 count, extreme proper times, and argument limits."""
 import numpy as np
@@ -38,13 +38,14 @@ def instances(n, seed):
                      np.exp(rng.uniform(np.log(0.02), np.log(3.0), n)))
 
 
+@pytest.mark.parametrize("nint", [4, 50])
 @pytest.mark.parametrize("n", [31, 32, 33, 127, 128, 129, 255, 256, 257, 513])
-def test_instance_counts_around_tile_sizes(ctx, n):
+def test_instance_counts_around_tile_sizes(ctx, n, nint):
     import wltube
 
     loops = O.vloops(31, 256, 64)
     cx, cy, T = instances(600, 17)
-    fld = wltube.field("smooth", fermion=1, nint=4)
+    fld = wltube.field("smooth", fermion=1, nint=nint)
     h = ctx.upload(loops)
     try:
         g_all, _, _ = ctx.eval(h, fld, cx, cy, T, [1.0, 2.0])
@@ -55,7 +56,7 @@ def test_instance_counts_around_tile_sizes(ctx, n):
         assert np.array_equal(g, g_all[:n])
     idx = [0, n // 2, n - 1]
     ref, S = O.eval_groups(loops, cx[idx], cy[idx], T[idx], [1.0, 2.0],
-                           O.field("smooth", fermion=1, nint=4), return_scale=True)
+                           O.field("smooth", fermion=1, nint=nint), return_scale=True)
     assert werr(g[idx], ref, S) < W_TOL
 
 
@@ -65,16 +66,17 @@ def test_points_per_loop_not_a_multiple_of_the_staging_chunk(ctx, ppl):
 
     loops = O.vloops(32, 256, ppl)
     cx, cy, T = instances(64, 3)
-    for prof, fe in (("smooth", 1), ("gaussian", 0)):
-        fld = wltube.field(prof, fermion=fe, nint=4)
+    for prof, fe, nint in (("smooth", 1, 4), ("gaussian", 0, 4), ("smooth", 0, 50),
+                           ("gaussian", 1, 50)):
+        fld = wltube.field(prof, fermion=fe, nint=nint)
         h = ctx.upload(loops)
         try:
             g, _, _ = ctx.eval(h, fld, cx, cy, T, [1.0])
         finally:
             ctx.release(h)
-        ref, S = O.eval_groups(loops, cx, cy, T, [1.0], O.field(prof, fermion=fe, nint=4),
+        ref, S = O.eval_groups(loops, cx, cy, T, [1.0], O.field(prof, fermion=fe, nint=nint),
                                return_scale=True)
-        assert werr(g, ref, S) < W_TOL, (prof, ppl)
+        assert werr(g, ref, S) < W_TOL, (prof, ppl, nint)
 
 
 def test_one_group_four_flux_values_extreme_proper_times(ctx):
