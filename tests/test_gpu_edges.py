@@ -1,8 +1,9 @@
 """Edge cases of the sweep through the C ABI: instance counts around the tile
 sizes (32 = loop-parallel threshold, 128 one-instance tiles, 256 pair
-tiles) at 4 and 50 intervals, loops whose point count is not a multiple of the 256-point staging
-chunk, the smallest loops (4 points), one group, the largest flux-value
-count, extreme proper times, and argument limits."""
+tiles) at 4 and 50 intervals, loops whose point count is not a multiple of
+the 256-point staging chunk, the smallest loops (4 points), one group, the
+largest flux-value count, extreme proper times, argument limits, and the
+bounded device wait."""
 import numpy as np
 import pytest
 
