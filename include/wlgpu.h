@@ -23,6 +23,40 @@
 #ifndef WLGPU_H
 #define WLGPU_H
 
+/* Legacy sources include intT.h first, whose profile names and constants
+ * (step, smooth, ..., profile, tubedist, lmin, q1, q2, ...) are object-like
+ * macros; they are set aside while this header is read and restored after. */
+#pragma push_macro("step")
+#undef step
+#pragma push_macro("smooth")
+#undef smooth
+#pragma push_macro("quadratic")
+#undef quadratic
+#pragma push_macro("gaussian")
+#undef gaussian
+#pragma push_macro("periodic")
+#undef periodic
+#pragma push_macro("spline")
+#undef spline
+#pragma push_macro("fixflux")
+#undef fixflux
+#pragma push_macro("profile")
+#undef profile
+#pragma push_macro("pi")
+#undef pi
+#pragma push_macro("tubedist")
+#undef tubedist
+#pragma push_macro("lmin")
+#undef lmin
+#pragma push_macro("q1")
+#undef q1
+#pragma push_macro("q2")
+#undef q2
+#pragma push_macro("Nspline")
+#undef Nspline
+#pragma push_macro("verbosity")
+#undef verbosity
+
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -380,5 +414,21 @@ int wl_legacy_query(int *profile, double *tubedist, double *lmin, int *nint, int
 #ifdef __cplusplus
 }
 #endif
+
+#pragma pop_macro("step")
+#pragma pop_macro("smooth")
+#pragma pop_macro("quadratic")
+#pragma pop_macro("gaussian")
+#pragma pop_macro("periodic")
+#pragma pop_macro("spline")
+#pragma pop_macro("fixflux")
+#pragma pop_macro("profile")
+#pragma pop_macro("pi")
+#pragma pop_macro("tubedist")
+#pragma pop_macro("lmin")
+#pragma pop_macro("q1")
+#pragma pop_macro("q2")
+#pragma pop_macro("Nspline")
+#pragma pop_macro("verbosity")
 
 #endif /* WLGPU_H */

@@ -2,6 +2,8 @@
 from the FP64 oracle: Tfunc's regimes and counterterms (Integrand.c:195-316),
 Simpson over ln T, Tintout's normalisation (Tint.c:69-72) and a jackknife
 over bins of loop groups."""
+import os
+
 import numpy as np
 import pytest
 
@@ -213,3 +215,40 @@ def test_legacy_integrateT_through_the_host_layer(capfd):
             assert abs(x - rho) < 1e-6 and np.isclose(leff, got.mean() / norm, rtol=1e-5)
     finally:
         wltube.legacy_configure("smooth")
+
+
+def test_c_driver_in_the_reference_style(tmp_path):
+    """A C program built the way the reference's drivers are (intT.h first,
+    then the library's headers; getwl, cudaMalloc/cudaMemcpy, struct Wparams,
+    integrateT) and linked with libwlhost.so + libwlgpu.so: its per-group
+    integrals against the oracle's integrateT, its Leffvsrho line against
+    their mean."""
+    import shutil
+    import subprocess
+
+    import wltube
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "worldline-flux-tube-lattice_gb300", "lib")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    exe = str(tmp_path / "legacy_driver")
+    subprocess.check_call(
+        ["gcc", "-O2", "-Wall", "-I" + os.path.join(root, "include"), "-I" + cuda + "/include",
+         os.path.join(root, "tests", "c", "legacy_driver.c"), "-o", exe, "-L" + libdir,
+         "-lwlhost", "-lwlgpu", "-L" + cuda + "/lib64", "-lcudart", "-lm",
+         "-Wl,-rpath," + libdir + ":" + cuda + "/lib64"])
+    loops = O.vloops(13, 256, 128)
+    txt = str(tmp_path / "loops.txt")
+    wltube.save_text_ensemble(txt, loops)
+    rho, F, l2 = 0.4, 1.0, 0.5
+    out = subprocess.check_output([exe, txt, "256", "128", str(rho), str(F), str(l2), "0", "4",
+                                   "40"], text=True).splitlines()
+    got = np.array([float(line.split()[2]) for line in out if line.startswith("I ")])
+    ref, _, _ = O.integrateT(loops, 40, rho, 0.0, F, O.field("smooth", fermion=0, nint=4,
+                                                              lambda2=l2))
+    se = ref.std(ddof=1) / np.sqrt(len(ref))
+    np.testing.assert_allclose(got, ref, rtol=0, atol=0.05 * se + 1e-12)
+    tag = [line for line in out if line.startswith("Leffvsrho:")]
+    assert len(tag) == 1
+    assert np.isclose(float(tag[0].split()[2]), got.mean() / (-2 * np.pi), rtol=1e-5)

@@ -231,6 +231,17 @@ def save_ensemble(path: str, loops: np.ndarray, seed: int = 0):
         raise OSError("cannot write ensemble file %s" % path)
 
 
+def save_text_ensemble(path: str, loops: np.ndarray, dim: int = 2):
+    """Write loops in the text format getwl reads (getwl.c:6-40): per loop
+    ppl x values, then ppl y values (and z for dim 3)."""
+    loops = np.ascontiguousarray(loops, dtype=np.float32)
+    Nl, ppl = loops.shape[:2]
+    H = host_lib()
+    H.wlh_putwl.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]
+    if H.wlh_putwl(loops.ctypes.data, path.encode(), Nl, ppl, dim) != 0:
+        raise OSError("cannot write %s" % path)
+
+
 def load_ensemble(path: str):
     """(loops [Nl][ppl][4] float32, seed) of a binary ensemble file."""
     nl, ppl, seed = C.c_int(), C.c_int(), C.c_uint64()
