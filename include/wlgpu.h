@@ -88,6 +88,10 @@ extern "C" {
  * quadrature per knot interval (the right-hand side does not depend on f). */
 #define WL_PROFILE_SPLINE 5
 #define WL_PROFILE_FIXFLUX 6
+/* wl_legacy_configure only: the fixflux profile with intEVff.cu's phi / chi
+ * fits (ff_variant 1), which the reference selects by linking intEVff.o
+ * instead of intEV.o; wl_legacy_query then reports WL_PROFILE_FIXFLUX. */
+#define WL_PROFILE_FIXFLUX_FF 7
 /* Square lattice of identical Gaussian flux tubes at R = a(m, n), |R| <=
  * rimage (no counterpart in the reference, whose "periodic" profile is a
  * radial shell model, intEV.cu:201-232): every image contributes the

@@ -248,6 +248,36 @@ def test_legacy_EV_matches_reference_golden(wl, gold):
     wl.legacy_configure("smooth")
 
 
+def test_legacy_EV_selects_the_intEVff_variant(ctx, wl):
+    """EV() for the fixflux profile with intEVff.cu's fits (the reference
+    links intEVff.o instead of intEV.o): every group's <W> equals wl_eval's
+    with ff_variant 1, and differs from the intEV.cu variant's."""
+    torch = pytest.importorskip("torch")
+    loops = O.vloops(14, 256, 128)
+    Nl, ppl = loops.shape[:2]
+    dev = torch.from_numpy(loops.reshape(-1)).cuda()
+    scal_d = torch.zeros(Nl * 4, device="cuda")
+    p = wl.Wparams()
+    p.Nl, p.Nppl, p.F, p.l2, p.fermion, p.ng = Nl, ppl, 1.0, 0.5, 0, Nl // 128
+    p.xcm.x, p.xcm.y = 1.1, 0.0
+    p.worldlines, p.Wsscal_d = dev.data_ptr(), scal_d.data_ptr()
+    T = 0.7
+    try:
+        res = {}
+        for name, ffv in (("fixflux-ff", 1), ("fixflux", 0)):
+            wl.legacy_configure(name, tubedist=2.0, nint=8)
+            res[ffv] = np.array([wl.EV(T, p, np.arange(g * 128, (g + 1) * 128))
+                                 for g in range(Nl // 128)])
+            h = ctx.upload(loops)
+            g, _, _ = ctx.eval(h, wl.field("fixflux", nint=8, lambda2=0.5, tubedist=2.0,
+                                           ff_variant=ffv), [1.1], [0.0], [T], [1.0])
+            ctx.release(h)
+            assert werr(res[ffv], g[0, 0]) < W_TOL, name
+        assert np.max(np.abs(res[1] - res[0])) > 1e-6
+    finally:
+        wl.legacy_configure("smooth")
+
+
 def test_legacy_EV_rejects_host_pointers(wl):
     p = wl.Wparams()
     loops = np.zeros((128, 8, 4), dtype=np.float32)

@@ -1561,7 +1561,9 @@ int wl_legacy_configure(int profile, double tubedist, double lmin, int nint, int
   LegacyState &L = legacy();
   std::lock_guard<std::mutex> lk(L.mu);
   wl_field f = L.field;
-  f.profile = profile;
+  const bool ff = profile == WL_PROFILE_FIXFLUX_FF;  // intEVff.cu's kernel
+  f.profile = ff ? WL_PROFILE_FIXFLUX : profile;
+  f.ff_variant = ff ? 1 : 0;
   f.tubedist = tubedist;
   f.lmin = lmin;
   f.nint = nint;

@@ -637,8 +637,10 @@ def eval_noalloc(dev_loops: int, Nl: int, ppl: int, fld: Field, ninst: int, dev_
 
 def legacy_configure(profile="smooth", tubedist=1.0, lmin=None, nint=50,
                      mode=MODE_REFCOMPAT):
+    """wl_legacy_configure: the profile EV() evaluates ("fixflux-ff": the
+    fixflux profile with intEVff.cu's fits)."""
     if isinstance(profile, str):
-        profile = PROFILES[profile]
+        profile = 7 if profile == "fixflux-ff" else PROFILES[profile]
     if lmin is None:
         lmin = 0.1 * tubedist
     st = lib().wl_legacy_configure(profile, tubedist, lmin, nint, mode)
