@@ -268,8 +268,6 @@ def run_batch(args):
     # plain per-instance kernel on a sample of instances of every job
     psegs, pms, pinst = 0, 0.0, 0
     for j in jobs:
-        if j["profile"] == "lattice":  # the plain kernel covers the single-tube profiles
-            continue
         idx = np.linspace(0, len(j["T"]) - 1, 2).astype(int)
         _, _, _, t = ctx.eval_plain(j["handle"], j["field"], j["cx"][idx], j["cy"][idx],
                                     j["T"][idx], j["F"], j["group"])
@@ -286,7 +284,7 @@ def run_batch(args):
         "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas},
         "plain_per_instance": {"value": plain, "unit": "segments/s",
                                "sample_instances": pinst, "device_ms": pms,
-                               "jobs": sum(j["profile"] != "lattice" for j in jobs)},
+                               "jobs": len(jobs)},
         "speedup_vs_plain": batched / plain,
         "config": {"workload": "uneven batch drawn as the 512-instance configuration "
                                "(seed 4), %d jobs, profiles %s, spinor, "

@@ -324,7 +324,8 @@ int wl_batch_stats(wl_ctx *ctx, double *device_ms, int *ntiles, int *grid,
 /* The plain per-instance kernel, the baseline of the batched path: one
  * launch per instance with one thread per loop walking its points from
  * global memory (the reference kernel's structure, intEV.cu:573-582), same
- * arithmetic and outputs as wl_eval.  *device_ms receives the summed time. */
+ * arithmetic and outputs as wl_eval; the step, smooth, quadratic, gaussian
+ * and lattice profiles.  *device_ms receives the summed time. */
 int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst,
                   const double *host_cx, const double *host_cy, const double *host_T,
                   int nF, const double *host_F, int group, double *out_group,

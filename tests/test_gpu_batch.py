@@ -115,3 +115,21 @@ def test_heavy_profiles_in_a_batch(setup):
     assert ctx.last_launches() == (2, "persistent-batch")
     for a_, b_ in zip(alone, outs[3]):
         np.testing.assert_array_equal(a_, b_)
+
+
+def test_plain_baseline_covers_the_lattice(setup):
+    """The plain per-instance kernel (one thread per loop, one launch per
+    instance) on the lattice profile: the same <W> as the batched path."""
+    import wltube
+
+    ctx, _, ens = setup
+    rng = np.random.default_rng(21)
+    cx, cy, T = f32_exact(rng.uniform(0, 5, 6), rng.uniform(0, 5, 6),
+                          np.exp(rng.uniform(np.log(0.05), np.log(2.0), 6)))
+    fld = wltube.field("lattice", fermion=1, nint=4, lambda2=1.0, tubedist=5.0)
+    h = ens[(128, 256)]
+    g, m, s, ms = ctx.eval_plain(h, fld, cx, cy, T, [1.0])
+    assert ms > 0 and ctx.last_launches() == (7, "plain-per-instance")
+    (gb, _, _), = ctx.batch_eval([{"handle": h, "field": fld, "cx": cx, "cy": cy, "T": T,
+                                   "F": [1.0], "group": 128}])
+    assert werr(g, gb) < W_TOL

@@ -1429,8 +1429,8 @@ int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst, con
   int r = eval_prologue(ctx, handle, field, ninst, nF, host_F, group, &e, &kprof, &fd);
   if (r) return r;
   if (!wl::plain_supports(kprof))
-    return fail(ctx, WL_ERR_INVALID, "the plain kernel covers the step, smooth, quadratic and "
-                                     "gaussian profiles");
+    return fail(ctx, WL_ERR_INVALID, "the plain kernel covers the step, smooth, quadratic, "
+                                     "gaussian and lattice profiles");
   if ((r = upload_instances(ctx, ninst, host_cx, host_cy, host_T, e.ppl))) return r;
   const int ng = e.Nl / group;
   const size_t npart = (size_t)e.Nl * nF * 3 * ninst;
@@ -1454,6 +1454,7 @@ int wl_eval_plain(wl_ctx *ctx, int handle, const wl_field *field, int ninst, con
   fill_flux(a, field, nF, host_F);
   a.field = fd;
   a.partial = ctx->partial.p;
+  if (kprof == wl::kLattice && (r = ensure_bbox(ctx, handle, &a.bbox))) return r;
   cudaEvent_t e0, e1;
   WL_CHECK(ctx, cudaEventCreate(&e0));
   WL_CHECK(ctx, cudaEventCreate(&e1));

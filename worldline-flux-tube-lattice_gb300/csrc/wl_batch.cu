@@ -167,6 +167,8 @@ __global__ void __launch_bounds__(128) plain_kernel(const __grid_constant__ Loop
   const df tq = {A.tqh[inst], A.tql[inst]};
   const FieldDev &F = A.field;
   const float4 *w = A.loops + (size_t)l * A.ppl;
+  ImgRange img = {0, -1, 0, -1, 1};  // lattice: this loop's images
+  if constexpr (P == kLattice) img = image_range(A.bbox[l], s, cx, cy, F);
   auto pt = [&](int p, float &x, float &y) {
     const float4 v = w[p];
     x = fmaf(s, v.x, cx);
@@ -178,7 +180,7 @@ __global__ void __launch_bounds__(128) plain_kernel(const __grid_constant__ Loop
   pt(1, z1x, z1y);
   pt(2, z2x, z2y);
   pt(3, z3x, z3y);
-  segment<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, ph[0], sp[0]);
+  seg<P, FERM, NINT>(z1x, z1y, z3x, z3y, F, img, ph[0], sp[0]);
   float zAx = z0x, zAy = z0y, zBx = z2x, zBy = z2y, zOx = z3x, zOy = z3y;
   for (int q = 1; q < A.ppl / 4; ++q) {
     float P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
@@ -186,17 +188,17 @@ __global__ void __launch_bounds__(128) plain_kernel(const __grid_constant__ Loop
     pt(4 * q + 1, P1x, P1y);
     pt(4 * q + 2, P2x, P2y);
     pt(4 * q + 3, P3x, P3y);
-    segment<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, ph[2], sp[2]);
-    segment<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, ph[0], sp[0]);
-    segment<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, ph[1], sp[1]);
-    segment<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, ph[0], sp[0]);
+    seg<P, FERM, NINT>(zAx, zAy, P0x, P0y, F, img, ph[2], sp[2]);
+    seg<P, FERM, NINT>(zOx, zOy, P1x, P1y, F, img, ph[0], sp[0]);
+    seg<P, FERM, NINT>(zBx, zBy, P2x, P2y, F, img, ph[1], sp[1]);
+    seg<P, FERM, NINT>(P1x, P1y, P3x, P3y, F, img, ph[0], sp[0]);
     zAx = P0x; zAy = P0y;
     zBx = P2x; zBy = P2y;
     zOx = P3x; zOy = P3y;
   }
-  segment<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, ph[0], sp[0]);
-  segment<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, ph[1], sp[1]);
-  segment<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, ph[2], sp[2]);
+  seg<P, FERM, NINT>(zOx, zOy, z1x, z1y, F, img, ph[0], sp[0]);
+  seg<P, FERM, NINT>(zBx, zBy, z2x, z2y, F, img, ph[1], sp[1]);
+  seg<P, FERM, NINT>(zAx, zAy, z0x, z0y, F, img, ph[2], sp[2]);
   const df G[3] = {df{ph[0], 0.f}, df{ph[1], 0.f}, df{ph[2], 0.f}};
   const df H[3] = {df{sp[0], 0.f}, df{sp[1], 0.f}, df{sp[2], 0.f}};
   loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
@@ -216,6 +218,7 @@ cudaError_t plain_dispatch(int kprof, const LoopArgs &a, int inst, cudaStream_t 
     case kGaussian: plain_kernel<kGaussian, FERM, NINT><<<grid, 128, 0, st>>>(a, inst); break;
     case kStep: plain_kernel<kStep, FERM, NINT><<<grid, 128, 0, st>>>(a, inst); break;
     case kQuadratic: plain_kernel<kQuadratic, FERM, NINT><<<grid, 128, 0, st>>>(a, inst); break;
+    case kLattice: plain_kernel<kLattice, FERM, NINT><<<grid, 128, 0, st>>>(a, inst); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -239,9 +242,7 @@ bool batch_supports(int kprof, int nint) {
 
 bool batch_in_kernel(int kprof) { return light_profile(kprof) || kprof == kLattice; }
 
-bool plain_supports(int kprof) {
-  return kprof == kSmooth || kprof == kGaussian || kprof == kStep || kprof == kQuadratic;
-}
+bool plain_supports(int kprof) { return light_profile(kprof) || kprof == kLattice; }
 
 int batch_max_ctas_per_sm() {
   int n = 0;
