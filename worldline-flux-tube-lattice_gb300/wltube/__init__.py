@@ -193,6 +193,8 @@ def host_lib():
         H.integrateT.restype = C.POINTER(C.c_double)
         H.Tfunc.argtypes = [C.c_double, vp, ip]
         H.Tfunc.restype = C.POINTER(C.c_double)
+        H.wlh_putwl.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, C.c_int]
+        H.getwl.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, C.c_int]
         _host = H
     return _host
 
@@ -236,9 +238,7 @@ def save_text_ensemble(path: str, loops: np.ndarray, dim: int = 2):
     ppl x values, then ppl y values (and z for dim 3)."""
     loops = np.ascontiguousarray(loops, dtype=np.float32)
     Nl, ppl = loops.shape[:2]
-    H = host_lib()
-    H.wlh_putwl.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]
-    if H.wlh_putwl(loops.ctypes.data, path.encode(), Nl, ppl, dim) != 0:
+    if host_lib().wlh_putwl(loops.ctypes.data, path.encode(), Nl, ppl, dim) != 0:
         raise OSError("cannot write %s" % path)
 
 
