@@ -86,3 +86,9 @@ def test_python_helpers_round_trip(tmp_path):
     wltube.save_ensemble(p, loops, seed=5)
     back, seed = wltube.load_ensemble(p)
     assert seed == 5 and np.array_equal(back, loops)
+    # the text format through the Python helper, read back by getwl (x, y)
+    t = str(tmp_path / "x.txt")
+    wltube.save_text_ensemble(t, loops)
+    back2 = np.zeros_like(loops)
+    assert wltube.host_lib().getwl(back2.ctypes.data, t.encode(), 4, 8, 2) == 0
+    assert np.array_equal(back2[..., :2], loops[..., :2]) and not back2[..., 2:].any()
