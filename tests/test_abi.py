@@ -66,3 +66,26 @@ def test_built_for_sm_103a_only():
     src = open(os.path.join(PKG, "build.py")).read()
     assert "arch=compute_103a,code=sm_103a" in src
     assert "sm_100" not in src and "sm_90" not in src
+
+
+@pytest.mark.parametrize("compiler", ["gcc", "g++"])
+def test_headers_compile_after_intT_h(tmp_path, compiler):
+    """A reference source includes intT.h first, whose profile names and
+    constants (smooth, profile, tubedist, lmin, ...) are object-like macros;
+    the library's headers must still compile after it, as C and as C++, and
+    leave those macros as intT.h defined them."""
+    src = tmp_path / "order.c"
+    src.write_text(
+        '#include "intT.h"\n#include "wlgpu.h"\n#include "wl_host.h"\n'
+        "int main(void) {\n"
+        "  double c = pi * q1 * q2 + tubedist + lmin;\n"
+        "  int p = profile;\n"
+        "  (void)c;\n"
+        "  return p == smooth && WL_PROFILE_FIXFLUX_FF == 7 ? 0 : 1;\n"
+        "}\n")
+    cuda_inc = "/usr/local/cuda/include"
+    cmd = [compiler, "-Wall", "-Werror", "-fsyntax-only", "-I" + INC, "-I" + cuda_inc]
+    if compiler == "g++":
+        cmd += ["-x", "c++"]
+    r = subprocess.run(cmd + [str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
