@@ -622,8 +622,9 @@ def main():
                     help="c2: the headline spinor workload; batch: uneven multi-job batch; "
                          "serve: Poisson request stream through the server")
     ap.add_argument("--jobs", type=int, default=32, help="jobs of the batch workload")
-    ap.add_argument("--batch-profiles", default="smooth,gaussian",
-                    help="profiles of the batch jobs (add lattice for lattice a = 5 lambda jobs)")
+    ap.add_argument("--batch-profiles", default="smooth,gaussian,lattice",
+                    help="profiles of the batch jobs (the configuration's mix: smooth, "
+                         "gaussian and lattice a = 5 lambda)")
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
     ap.add_argument("--lattice-grid", type=int, default=32,
                     help="centres per side of the unit cell (lattice workload)")
