@@ -260,7 +260,9 @@ int wl_spline_table(double lambda2, double tubedist, int n, float *rho2, float *
  * call before any stream capture.  Runs on `stream` (a cudaStream_t, NULL for
  * the default stream) and returns when the outputs are written.  All calls
  * share the one array, which keeps the last call's contents: calls that
- * overlap on the GPU (other host threads, other streams) race. */
+ * overlap on the GPU (other host threads, other streams) race.  The lattice
+ * and spline profiles are refused (WL_ERR_INVALID): they need per-loop
+ * bounding boxes or a profile table that the library would allocate. */
 int wl_eval_noalloc(const float *dev_loops, int Nl, int ppl, const wl_field *field,
                     int ninst, const double *dev_cx, const double *dev_cy,
                     const double *dev_T, int nF, const double *host_F, int group,
@@ -415,6 +417,18 @@ int wl_legacy_configure(int profile, double tubedist, double lmin, int nint,
                         int mode);
 /* the configuration EV() uses (any pointer may be NULL) */
 int wl_legacy_query(int *profile, double *tubedist, double *lmin, int *nint, int *mode);
+/* EV() keeps the per-loop W factors of its last (T, x_cm, F, lambda^2,
+ * fermion, configuration, ensemble pointer and shape) so that the ng group
+ * calls of one Tfunc (Integrand.c:249-305) cost one sweep.  A call for the
+ * first group of 128 consecutive loops, or for any other index list, also
+ * compares a 64-bit fingerprint of the ensemble's coordinates with the one
+ * the cached sweep read, and recomputes if the loops were rewritten in
+ * place.  Calls for the other consecutive groups at an unchanged key trust
+ * the cache; a caller that rewrites the ensemble between those calls calls
+ * wl_legacy_invalidate() (the next EV() call recomputes).  No counterpart in
+ * the reference, whose EV() relaunches its kernel on every call
+ * (intEV.cu:123). */
+int wl_legacy_invalidate(void);
 
 #ifdef __cplusplus
 }

@@ -250,6 +250,55 @@ def werr(w, ref, scale, floor=1e-2):
     return np.max(np.abs(np.asarray(w) - ref) / np.maximum(np.abs(ref), floor * scale))
 
 
+W_FLOOR = 1e-2   # floor of the relative error, in units of S
+STRICT_FT = 10.0  # F * T' up to which FP32 segment phases meet 1e-5 under that floor
+
+
+def accuracy(groups, ref, S, F, T, floor=W_FLOOR):
+    """Error of per-group <W> (groups, ref, S: [ninst][nF][ng]) against the
+    FP64 oracle, stated three ways:
+      rel       |W - W64| / max(|W64|, floor S) per (instance, F, group);
+      strict    the same restricted to F T' <= STRICT_FT (or F <= 0.1), where
+                FP32 segment arithmetic reaches 1e-5;
+      mc        |mean - mean64| / SEM64 per (instance, F): the error of the
+                ensemble mean in units of its Monte Carlo error bar (the SEM
+                over groups, as the reference's Tintout reports it), stated
+                for the pairs whose relative error exceeds 1e-5 (at weak
+                fields the SEM itself falls to ~1e-12 while the relative
+                error is ~1e-12 too).
+    Returns a dict of the maxima, counts and the floor."""
+    groups, ref, S = np.asarray(groups), np.asarray(ref), np.asarray(S)
+    F, T = np.asarray(F, np.float64), np.asarray(T, np.float64)
+    rel = np.abs(groups - ref) / np.maximum(np.abs(ref), floor * S)
+    per = rel.max(axis=2)  # [ninst][nF]
+    strict = (F[None, :] * T[:, None] <= STRICT_FT) | (F[None, :] <= 0.1 + 1e-12)
+    ng = ref.shape[2]
+    m64 = ref.mean(axis=2)
+    sem64 = ref.std(axis=2, ddof=1) / np.sqrt(ng)
+    dm = np.abs(groups.mean(axis=2) - m64)
+    mc = dm / np.maximum(sem64, 1e-300)
+    return {
+        "metric": "|W-W64|/max(|W64|, %g*S) per group, S = 8/3<|w_N|> + 2<|w_N/2|> + "
+                  "1/3<|w_N/4|>" % floor,
+        "floor": floor,
+        "pairs": int(per.size),
+        "max_rel": float(per.max()),
+        "median_rel": float(np.median(per)),
+        "within_1e-5": int((per <= 1e-5).sum()),
+        "strict_region": "F*T <= %g or F <= 0.1" % STRICT_FT,
+        "strict_pairs": int(strict.sum()),
+        "max_rel_strict": float(per[strict].max()) if strict.any() else None,
+        "max_rel_by_F": {("%g" % f): float(per[:, j].max()) for j, f in enumerate(F)},
+        "max_err_over_sem": float(mc.max()),
+        "beyond_1e-5": int((per > 1e-5).sum()),
+        "max_err_over_sem_beyond_1e-5": float(mc[per > 1e-5].max()) if (per > 1e-5).any()
+        else None,
+        "per_pair": per,
+        "mc": mc,
+        "strict_mask": strict,
+    }
+
+
 def magfield(rho2, F, fld):
     return lib().wlo_magfield(rho2, F, C.byref(fld), C.byref(QED))
 

@@ -66,7 +66,24 @@ def test_scalar_configuration_full_size(ctx):
 
 def test_spinor_configuration_full_size(ctx):
     """Spinor QED, smooth tube, F in {0.1, 1, 10}: Nl 5120 x ppl 2048 (seed 2),
-    128 log T in [1e-3, 1e3] x 64 rho in [0, 8] -- the benchmark workload."""
+    128 log T in [1e-3, 1e3] x 64 rho in [0, 8] -- the benchmark workload.
+
+    The FP64 oracle checks 128 instances that cover every one of the 128
+    proper times and every radius (twice each), at all three flux values.
+    Accuracy is asserted as stated for this path:
+      * |W - W64| <= 1e-5 max(|W64|, 1e-2 S) per group wherever F T' <= 10
+        (or F <= 0.1): there the FP32 segment phases reach the tolerance;
+      * wherever that relative error exceeds 1e-5, the error of the ensemble
+        mean is below 1 % of its Monte Carlo error bar (the SEM over groups),
+        and everywhere the per-group error stays below 1e-2 of
+        max(|W64|, 1e-2 S).  Beyond F T' = 10 the FP32 rounding
+        of each segment's phase contribution (1e-7 relative, summed over ~10^3
+        segments whose contributions cancel to a phase of at most ~60) gives
+        phase errors of ~1e-5 rad, which the floor 1e-2 S turns into
+        relative errors up to ~1e-3; the spin exponents are not the limit.
+    No loop of this configuration reaches the reference's 600 sentinel
+    (Integrand.c:371-377; the largest cosh argument over the checked
+    instances is about 220); test_gpu_parity covers the sentinel regime."""
     import wltube
 
     Nl, ppl = 5120, 2048
@@ -81,13 +98,23 @@ def test_spinor_configuration_full_size(ctx):
     sub = np.arange(3, 8192, 97)
     g1, _, _ = ctx.eval(h, fld, cx[sub], cy[sub], T[sub], F)
     assert np.array_equal(g1, g[sub])
-    # the oracle on instances with spin exponents below ~25 (T <= 4, F <= 1)
-    pick = [r * 128 + k for r in (0, 16, 63) for k in (0, 30, 55, 64, 72)]
+    # the oracle on every proper time and every radius, all three F
+    k = np.arange(128)
+    pick = (k * 37 % 64) * 128 + k
+    assert len(set(pick % 128)) == 128 and len(set(pick // 128)) == 64
     loops = ctx.download(h)
-    ref, S = O.eval_groups(loops, cx[pick], cy[pick], T[pick], F[:2],
+    ref, S = O.eval_groups(loops, cx[pick], cy[pick], T[pick], F,
                            O.field("smooth", fermion=1, nint=4), return_scale=True)
-    assert np.all(T[pick] <= 4.0)
-    assert werr(g[pick, :2], ref, S).max() < W_TOL
+    acc = O.accuracy(g[pick], ref, S, F, T[pick])
+    print({k: v for k, v in acc.items() if not isinstance(v, np.ndarray)})
+    assert acc["strict_pairs"] >= 150
+    assert acc["max_rel_strict"] <= W_TOL, acc["max_rel_strict"]
+    beyond = acc["max_err_over_sem_beyond_1e-5"]
+    assert beyond is None or beyond <= 1e-2, beyond
+    assert acc["max_rel"] <= 1e-2, acc["max_rel"]
+    assert acc["max_rel_by_F"]["0.1"] <= W_TOL
+    # the mean / SEM outputs of the picked instances against the oracle's
+    np.testing.assert_allclose(mean[pick], g[pick].mean(axis=2), rtol=1e-13, atol=0)
     ctx.release(h)
 
 

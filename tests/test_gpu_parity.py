@@ -132,10 +132,10 @@ def _instances(n, rho_max, Tlo, Thi, seed):
     # a finite amount -- the spinor result is discontinuous in its inputs
     ("step", 1, 4, 2.0, 1e-3)])
 def test_batched_eval_matches_oracle(ctx, wl, prof, fe, nint, l2, tol):
-    # T <= 4 and F <= 1.5 keep the spin exponents below ~25: beyond that the
-    # FP32 rounding of the loop points alone (2^-24 |psi| per loop, carried by
-    # the few loops that dominate an average of cosh) exceeds 1e-5 -- see
-    # test_strong_spin_factor_error_is_fp32_limited
+    # T <= 4 and F <= 1.5 keep F T' <= 6: beyond F T' ~ 10 the FP32 rounding
+    # of each segment's phase contribution (summed over loops whose segment
+    # contributions cancel) gives phase errors that the 1e-2 S floor turns
+    # into more than 1e-5 -- see test_strong_field_error_is_fp32_limited
     loops = O.vloops(2, 256, 256)
     cx, cy, T = _instances(160, 3.0, 0.01, 4.0, 7)
     F = [0.1, 1.0, 1.5]
@@ -154,9 +154,13 @@ def test_batched_eval_matches_oracle(ctx, wl, prof, fe, nint, l2, tol):
     assert np.all(np.abs(mean - ref.mean(axis=2)) <= budget)
 
 
-def test_strong_spin_factor_error_is_fp32_limited(ctx, wl):
-    """With spin exponents up to ~100 the error against FP64 follows the FP32
-    rounding of the exponents: |dW| <= 1e-5 max(|W|, 1e-2 S) (1 + psi_max/25)."""
+def test_strong_field_error_is_fp32_limited(ctx, wl):
+    """With F T' up to 30 (spin exponents up to ~60) the error against FP64
+    grows with the field: |dW| <= 1e-5 max(|W|, 1e-2 S) (1 + 2 F T'/25).
+    The FP32 segment phases set it (their absolute error, ~1e-7 of the sum of
+    the segment contributions' magnitudes, is amplified 100-fold by the floor
+    wherever the cosines of the dominant loops are small); the spin exponents'
+    FP32 error contributes an order of magnitude less."""
     loops = O.vloops(2, 256, 256)
     cx, cy, T = _instances(96, 1.0, 1.0, 10.0, 9)
     F = [1.0, 3.0]
@@ -168,10 +172,73 @@ def test_strong_spin_factor_error_is_fp32_limited(ctx, wl):
         ctx.release(h)
     ofld = O.field("smooth", fermion=1, nint=4)
     ref, S = O.eval_groups(loops, cx, cy, T, F, ofld, return_scale=True)
-    # largest spin exponent per (instance, F): 2 F T f'(rho^2) <= 2 F T / lambda^2
+    # 2 F T' (the largest spin exponent, 2 F T' f'(0) with lambda = 1)
     psi = 2.0 * np.asarray(F)[None, :, None] * T[:, None, None]
     err = np.abs(g - ref) / np.maximum(np.abs(ref), W_FLOOR * S)
     assert np.all(err <= W_TOL * (1.0 + psi / 25.0))
+
+
+def test_cosh_sentinel_regime_matches_oracle(ctx, wl):
+    """The reference's large-cosh sentinel (Integrand.c:371-377): a loop whose
+    int-truncated N/2 spin exponent or N/4 sum exceeds 600 gets its three W
+    factors multiplied by 1e10 instead of by cosh.  A wide smooth tube
+    (lambda^2 = 100) at F = 50, rho = 0, T = 2000 (eB = 1 at the axis, as
+    testT.c:20 sets it) gives ten such loops among 256 beside loops with
+    cosh arguments up to ~350.  Per loop (EV() over a list of one loop
+    repeated, the W factors of the loop-parallel kernel) the result equals
+    the oracle's EVMean of that loop: 1e10 times the Richardson sum of its
+    cosines for the sentinel loops, the cos * cosh sum for the others; and
+    the group <W> of the instance-parallel sweep matches the oracle."""
+    torch = pytest.importorskip("torch")
+    loops = O.vloops(8, 256, 256)
+    Nl, ppl = loops.shape[:2]
+    l2, F = 100.0, 50.0
+    cx, cy, T = f32_exact([0.0], [0.0], [2000.0])
+    ofld = O.field("smooth", fermion=1, nint=4, lambda2=l2)
+    s64, f64 = O.loops_phases(loops, cx[0], cy[0], T[0], F, ofld)
+    nb4 = f64[:, 1] + f64[:, 2]
+    sent = (np.trunc(np.abs(nb4)) > 600) | (np.trunc(np.abs(f64[:, 0])) > 600)
+    assert 3 <= sent.sum() <= 40
+    # no loop within reach of the truncation edge (FP32 exponent error ~1e-4)
+    assert np.min(np.abs(np.abs(np.concatenate([nb4, f64[:, 0]])) - 601.0)) > 1e-2
+    args = np.stack([0.5 * f64[:, 0] + 0.25 * nb4, f64[:, 0], 0.5 * nb4], 1)
+    order = np.argsort(-np.abs(args).max(axis=1) * ~sent)
+    check = list(np.flatnonzero(sent)[:4]) + list(order[:4])
+    dev = torch.from_numpy(loops.reshape(-1)).cuda()
+    scal_d = torch.zeros(Nl * 4, device="cuda")
+    ferm_d = torch.zeros(Nl * 4, device="cuda")
+    p = wl.Wparams()
+    p.Nl, p.Nppl, p.F, p.l2, p.fermion, p.ng = Nl, ppl, F, l2, 1, Nl // 128
+    p.xcm.x, p.xcm.y = float(cx[0]), float(cy[0])
+    p.worldlines, p.Wsscal_d, p.Wsferm_d = dev.data_ptr(), scal_d.data_ptr(), ferm_d.data_ptr()
+    try:
+        wl.legacy_configure("smooth", nint=4)
+        for l in check:
+            got = wl.EV(float(T[0]), p, np.full(128, l))
+            w = O.wfactors(s64[l], f64[l], 1)
+            ref = 8 / 3 * w[0] - 2 * w[1] + 1 / 3 * w[2]
+            # each factor's size without its cosine (1e10, or cosh of its
+            # argument); the kernel's phases are good to ~1e-5 rad and its
+            # spin exponents to ~1e-7 relative: tolerance 1e-4 rad and 1e-6
+            # of the argument
+            size = np.full(3, 1e10) if sent[l] else np.cosh(args[l])
+            err_k = 1e-4 + (0.0 if sent[l] else 1e-6 * np.abs(args[l]))
+            tol = np.dot([8 / 3, 2.0, 1 / 3], size * err_k)
+            assert abs(got - ref) <= tol, (int(l), bool(sent[l]), got, ref)
+            if sent[l]:
+                assert abs(got) <= 5.1e10  # 1e10 times cosines: the sentinel fired
+            else:
+                assert abs(got) > 1e20     # cosh of an argument above 50
+    finally:
+        wl.legacy_configure("smooth")
+    h = ctx.upload(loops)
+    try:
+        g, _, _ = ctx.eval(h, wl.field("smooth", fermion=1, nint=4, lambda2=l2), cx, cy, T, [F])
+    finally:
+        ctx.release(h)
+    ref, S = O.eval_groups(loops, cx, cy, T, [F], ofld, return_scale=True)
+    assert np.all(np.isfinite(g))
+    assert werr(g, ref, S) <= 1e-2
 
 
 def test_loop_parallel_eval_matches_oracle(ctx, wl):
@@ -278,6 +345,51 @@ def test_legacy_EV_selects_the_intEVff_variant(ctx, wl):
         wl.legacy_configure("smooth")
 
 
+def test_legacy_EV_sees_an_ensemble_rewritten_in_place(wl):
+    """EV() caches the sweep of its last (T, x_cm, ...) key; a caller that
+    rewrites the loops in place and calls again at the same key gets the new
+    loops' <W>: the first group's call compares the ensemble's fingerprint,
+    and wl_legacy_invalidate() drops the cache for the other groups."""
+    torch = pytest.importorskip("torch")
+    a = O.vloops(31, 256, 128)
+    b = O.vloops(32, 256, 128)
+    Nl, ppl = a.shape[:2]
+    dev = torch.from_numpy(a.reshape(-1).copy()).cuda()
+    scal_d = torch.zeros(Nl * 4, device="cuda")
+    p = wl.Wparams()
+    p.Nl, p.Nppl, p.F, p.l2, p.fermion, p.ng = Nl, ppl, 1.0, 1.0, 0, Nl // 128
+    p.xcm.x, p.xcm.y = 0.4, 0.0
+    p.worldlines, p.Wsscal_d = dev.data_ptr(), scal_d.data_ptr()
+    T = 1.3
+    g0, g1 = np.arange(128), np.arange(128, 256)
+    fld = O.field("smooth", fermion=0, nint=50)
+    cx, _, Tp = f32_exact([0.4], [0.0], [T])
+    ref_a = O.eval_groups(a, cx, 0.0, Tp, [1.0], fld)[0, 0]
+    ref_b = O.eval_groups(b, cx, 0.0, Tp, [1.0], fld)[0, 0]
+    try:
+        wl.legacy_configure("smooth", nint=50)
+        got_a = [wl.EV(T, p, g0), wl.EV(T, p, g1)]
+        np.testing.assert_allclose(got_a, ref_a, rtol=W_TOL)
+        # rewrite in place, same key: the first group's call notices
+        dev.copy_(torch.from_numpy(b.reshape(-1).copy()).cuda())
+        torch.cuda.synchronize()
+        got_b0 = wl.EV(T, p, g0)
+        np.testing.assert_allclose(got_b0, ref_b[0], rtol=W_TOL)
+        np.testing.assert_allclose(wl.EV(T, p, g1), ref_b[1], rtol=W_TOL)
+        # rewrite back, then ask for the second group first: invalidate
+        dev.copy_(torch.from_numpy(a.reshape(-1).copy()).cuda())
+        torch.cuda.synchronize()
+        wl.legacy_invalidate()
+        np.testing.assert_allclose(wl.EV(T, p, g1), ref_a[1], rtol=W_TOL)
+        # any non-consecutive list also checks the fingerprint
+        dev.copy_(torch.from_numpy(b.reshape(-1).copy()).cuda())
+        torch.cuda.synchronize()
+        rot = wl.EV(T, p, np.roll(g1, 3))
+        np.testing.assert_allclose(rot, ref_b[1], rtol=W_TOL)
+    finally:
+        wl.legacy_configure("smooth")
+
+
 def test_legacy_EV_rejects_host_pointers(wl):
     p = wl.Wparams()
     loops = np.zeros((128, 8, 4), dtype=np.float32)
@@ -324,7 +436,7 @@ def test_lattice_matches_oracle(ctx, wl, a, l2, fe):
         ctx.release(h)
     ofld = O.field("lattice", fermion=fe, nint=4, mode=1, lambda2=l2, tubedist=a)
     ref, S = O.eval_groups(loops, cx, cy, T, [1.0], ofld, return_scale=True)
-    # the FP32 spin-exponent limit of test_strong_spin_factor_error_is_fp32_limited
+    # the FP32 limit of test_strong_field_error_is_fp32_limited
     psi = np.array([np.abs(O.loops_phases(loops, x, y, t, 1.0, ofld)[1]).max() if fe else 0.0
                     for x, y, t in zip(cx, cy, T)])
     err = np.abs(g - ref) / np.maximum(np.abs(ref), W_FLOOR * S)

@@ -79,3 +79,54 @@ def test_noalloc_rejects_requests_beyond_its_scratch():
                             d.data_ptr(), d.data_ptr(), d.data_ptr(), [1.0, 1.0, 1.0, 1.0],
                             128, 0, out.data_ptr(), 0)
     assert e.value.status == -1
+
+
+def test_noalloc_matches_the_oracle():
+    """The allocation-free entry point against the FP64 oracle directly, at
+    the tolerance of the other GPU tests, for a scalar and a spinor field."""
+    torch = pytest.importorskip("torch")
+    import wltube
+
+    rng = np.random.default_rng(7)
+    Nl, ppl, group, ninst = 256, 256, 128, 64
+    loops = O.vloops(17, Nl, ppl)
+    rt = np.sqrt(np.exp(rng.uniform(np.log(0.01), np.log(4.0), ninst))).astype(np.float32)
+    cx = rng.uniform(0.0, 3.0, ninst).astype(np.float32).astype(np.float64)
+    cy = rng.uniform(-0.2, 0.2, ninst).astype(np.float32).astype(np.float64)
+    T = rt.astype(np.float64) ** 2
+    F = [0.1, 1.0]
+    dev = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    dloops = torch.from_numpy(loops.reshape(-1)).cuda()
+    dcx, dcy, dT = dev(cx), dev(cy), dev(T)
+    ng = Nl // group
+    for prof, fe in (("smooth", 1), ("gaussian", 0)):
+        out = torch.full((ninst * len(F) * ng,), np.nan, dtype=torch.float64, device="cuda")
+        wltube.eval_noalloc(dloops.data_ptr(), Nl, ppl, wltube.field(prof, fermion=fe, nint=4),
+                            ninst, dcx.data_ptr(), dcy.data_ptr(), dT.data_ptr(), F, group,
+                            out.data_ptr(), 0, 0)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().reshape(ninst, len(F), ng)
+        ref, S = O.eval_groups(loops, cx, cy, T, F, O.field(prof, fermion=fe, nint=4),
+                               return_scale=True)
+        assert O.werr(got, ref, S, floor=W_FLOOR) <= W_TOL, prof
+
+
+@pytest.mark.parametrize("prof", ["lattice", "spline"])
+def test_noalloc_refuses_fields_that_need_library_memory(prof):
+    """The lattice profile needs per-loop bounding boxes and the spline
+    profile a table, both of which the library would allocate: refused with
+    WL_ERR_INVALID before any launch, leaving the outputs untouched."""
+    torch = pytest.importorskip("torch")
+    import wltube
+
+    Nl, ppl, ninst = 128, 16, 4
+    dloops = torch.zeros(Nl * ppl * 4, dtype=torch.float32, device="cuda")
+    d = torch.ones(ninst, dtype=torch.float64, device="cuda")
+    out = torch.full((ninst,), 7.0, dtype=torch.float64, device="cuda")
+    with pytest.raises(wltube.WlError) as e:
+        wltube.eval_noalloc(dloops.data_ptr(), Nl, ppl,
+                            wltube.field(prof, nint=4, tubedist=2.0), ninst,
+                            d.data_ptr(), d.data_ptr(), d.data_ptr(), [1.0], 128, 0,
+                            out.data_ptr(), 0)
+    assert e.value.status == -1
+    assert torch.all(out == 7.0)

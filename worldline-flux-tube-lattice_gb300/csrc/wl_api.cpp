@@ -360,6 +360,9 @@ struct LegacyState {
   // computed once per (T, x_cm) so that their EV() calls need no device work
   DevBuf<double> gres;
   std::vector<double> gev;
+  // fingerprint of the cached sweep's ensemble coordinates, and its scratch
+  unsigned long long fp = 0;
+  DevBuf<unsigned long long> fpd;
 };
 LegacyState &legacy() {
   static LegacyState s;
@@ -1557,7 +1560,11 @@ int wl_last_launches(wl_ctx *ctx, int *launches, const char **kind) {
 // Wsscal_h / Wsferm_h, then returns the Richardson-combined mean over the
 // 128 loops of WLlist.  The per-loop W factors of the last (T, xcm, field)
 // stay cached on the device, so the ng calls of one Tfunc() evaluation
-// (Integrand.c:249-305) cost one sweep and ng list reductions.
+// (Integrand.c:249-305) cost one sweep and ng list reductions.  The cache
+// also holds a 64-bit fingerprint of the ensemble's coordinates: a call for
+// the first group, or for any non-consecutive list, recomputes when the
+// loops were rewritten in place (the reference recomputes on every call,
+// intEV.cu:123); wl_legacy_invalidate() drops the cache outright.
 int wl_legacy_configure(int profile, double tubedist, double lmin, int nint, int mode) {
   LegacyState &L = legacy();
   std::lock_guard<std::mutex> lk(L.mu);
@@ -1576,6 +1583,13 @@ int wl_legacy_configure(int profile, double tubedist, double lmin, int nint, int
   if (r) return r;
   L.field = f;
   L.config_gen++;
+  L.valid = false;
+  return WL_OK;
+}
+
+int wl_legacy_invalidate(void) {
+  LegacyState &L = legacy();
+  std::lock_guard<std::mutex> lk(L.mu);
   L.valid = false;
   return WL_OK;
 }
@@ -1621,13 +1635,31 @@ double EV(double T, void *p, int *WLlist) {
   FieldDev fd;
   if (field_to_dev(ctx, &f, &kprof, &fd)) return legacy_fail(ctx->err.c_str());
   if (kprof == wl::kSpline && ensure_spline(ctx, &f, &fd)) return legacy_fail(ctx->err.c_str());
-  const bool hit = L.valid && L.T == T && L.F == params.F && L.l2 == params.l2 &&
-                   L.cx == params.xcm.x && L.cy == params.xcm.y &&
-                   L.loops == params.worldlines && L.Nl == params.Nl && L.ppl == params.Nppl &&
-                   L.fermion == f.fermion && L.gen == L.config_gen;
+  const size_t npts = (size_t)params.Nl * params.Nppl;
+  bool hit = L.valid && L.T == T && L.F == params.F && L.l2 == params.l2 &&
+             L.cx == params.xcm.x && L.cy == params.xcm.y &&
+             L.loops == params.worldlines && L.Nl == params.Nl && L.ppl == params.Nppl &&
+             L.fermion == f.fermion && L.gen == L.config_gen;
+  // a group of consecutive loops g*128 .. g*128+127 (what Tfunc passes)
+  bool consecutive = WLlist[0] % groupsize == 0;
+  for (int j = 1; j < groupsize && consecutive; ++j) consecutive = WLlist[j] == WLlist[0] + j;
+  if (hit && (!consecutive || WLlist[0] == 0)) {
+    // the first group of a Tfunc sweep, or any other list: check that the
+    // loops were not rewritten in place since the cached sweep read them
+    unsigned long long fp = 0;
+    cudaError_t ce = L.fpd.reserve(1);
+    if (ce == cudaSuccess) ce = wl::launch_fingerprint(params.worldlines, npts, L.fpd.p, ctx->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(&fp, L.fpd.p, sizeof(fp), cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+    if (ce != cudaSuccess) {
+      L.valid = false;
+      return legacy_fail(cudaGetErrorString(ce));
+    }
+    hit = fp == L.fp;
+  }
   if (!hit) {
     L.valid = false;
-    const size_t npts = (size_t)params.Nl * params.Nppl;
     if (check_device_range(ctx, params.worldlines, npts * sizeof(float4), "worldlines") ||
         check_device_range(ctx, params.Wsscal_d, params.Nl * sizeof(float4), "Wsscal_d") ||
         (f.fermion &&
@@ -1653,7 +1685,12 @@ double EV(double T, void *p, int *WLlist) {
     a.partial = L.w.p;
     a.scal = params.Wsscal_d;
     a.ferm = f.fermion ? params.Wsferm_d : nullptr;
-    cudaError_t ce = wl::launch_loopwarp(kprof, f.fermion != 0, f.nint, a, ctx->stream);
+    unsigned long long fp = 0;
+    cudaError_t ce = L.fpd.reserve(1);
+    if (ce == cudaSuccess) ce = wl::launch_fingerprint(params.worldlines, npts, L.fpd.p, ctx->stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(&fp, L.fpd.p, sizeof(fp), cudaMemcpyDeviceToHost, ctx->stream);
+    if (ce == cudaSuccess) ce = wl::launch_loopwarp(kprof, f.fermion != 0, f.nint, a, ctx->stream);
     if (ce == cudaSuccess && params.Wsscal_h)
       ce = cudaMemcpyAsync(params.Wsscal_h, params.Wsscal_d, params.Nl * sizeof(float4),
                            cudaMemcpyDeviceToHost, ctx->stream);
@@ -1683,11 +1720,10 @@ double EV(double T, void *p, int *WLlist) {
     L.ppl = params.Nppl;
     L.fermion = f.fermion;
     L.gen = L.config_gen;
+    L.fp = fp;
     L.valid = true;
   }
   // a group of consecutive loops: its mean is already on the host
-  bool consecutive = WLlist[0] % groupsize == 0;
-  for (int j = 1; j < groupsize && consecutive; ++j) consecutive = WLlist[j] == WLlist[0] + j;
   if (consecutive && (size_t)(WLlist[0] / groupsize) < L.gev.size())
     return L.gev[(size_t)(WLlist[0] / groupsize)];
   if (ctx->list.reserve(groupsize) != cudaSuccess || L.res.reserve(1) != cudaSuccess)

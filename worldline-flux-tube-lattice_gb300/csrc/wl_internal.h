@@ -170,6 +170,11 @@ cudaError_t launch_tint(const TintArgs &a, cudaStream_t s);
 cudaError_t launch_order_instances(const float *cx, const float *cy, const float *rtT, int n,
                                    float inv_a, int *perm, cudaStream_t s);
 
+// 64-bit fingerprint of the (x, y) coordinates of npts float4 points (zeroes
+// *out first; EV()'s check that a cached ensemble was not rewritten)
+cudaError_t launch_fingerprint(const float4 *loops, size_t npts, unsigned long long *out,
+                               cudaStream_t s);
+
 // per-loop bounding boxes of an ensemble (lattice image selection)
 cudaError_t launch_loop_bbox(const float4 *loops, int Nl, int ppl, float4 *out, cudaStream_t s);
 

@@ -259,6 +259,48 @@ __global__ void loop_bbox_kernel(const float4 *__restrict__ loops, int Nl, int p
   if (lane == 0) out[l] = make_float4(x0, x1, y0, y1);
 }
 
+// ------------------------------------------------------- fingerprint --
+// Content fingerprint of an ensemble's (x, y) coordinates: the sum modulo
+// 2^64 of the splitmix64 finaliser (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014) applied to each point's
+// coordinate bits combined with its index.  Any change of a coordinate
+// changes the sum except with probability ~2^-64; the sum does not depend on
+// the order in which the points are added.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256)
+    fingerprint_kernel(const float2 *__restrict__ pts, size_t npts,
+                       unsigned long long *__restrict__ out) {
+  unsigned long long acc = 0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < npts; p += stride) {
+    const float2 v = pts[2 * p];  // (x, y) of the float4 point p
+    const unsigned long long bits =
+        (unsigned long long)__float_as_uint(v.x) |
+        ((unsigned long long)__float_as_uint(v.y) << 32);
+    acc += mix64(bits ^ mix64(p + 0x9e3779b97f4a7c15ull));
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+cudaError_t launch_fingerprint(const float4 *loops, size_t npts, unsigned long long *out,
+                               cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(*out), s);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t want = (npts + 255) / 256;
+  const int grid = (int)(want < (size_t)(sms * 8) ? (want > 0 ? want : 1) : (size_t)(sms * 8));
+  fingerprint_kernel<<<grid, 256, 0, s>>>(reinterpret_cast<const float2 *>(loops), npts, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_loop_bbox(const float4 *loops, int Nl, int ppl, float4 *out, cudaStream_t s) {
   const int warps = 4;
   loop_bbox_kernel<<<(Nl + warps - 1) / warps, warps * 32, 0, s>>>(loops, Nl, ppl, out);

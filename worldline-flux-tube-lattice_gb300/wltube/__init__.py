@@ -163,6 +163,7 @@ def lib():
                                C.c_double, C.c_double, fp, fp]
         L.wl_last_launches.argtypes = [vp, ip, C.POINTER(C.c_char_p)]
         L.wl_legacy_configure.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, C.c_int]
+        L.wl_legacy_invalidate.argtypes = []
         L.wl_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
         L.wl_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_longlong)]
         L.wl_server_wait.argtypes = [vp, C.c_longlong, C.c_double]
@@ -646,6 +647,13 @@ def legacy_configure(profile="smooth", tubedist=1.0, lmin=None, nint=50,
     st = lib().wl_legacy_configure(profile, tubedist, lmin, nint, mode)
     if st != 0:
         raise WlError(st, "wl_legacy_configure")
+
+
+def legacy_invalidate():
+    """wl_legacy_invalidate: the next EV() call recomputes its sweep."""
+    st = lib().wl_legacy_invalidate()
+    if st != 0:
+        raise WlError(st, "wl_legacy_invalidate")
 
 
 def EV(T: float, params: Wparams, WLlist) -> float:
