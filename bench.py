@@ -13,9 +13,16 @@ loops.  One step = one pass over all 8192 (rho, T) instances:
 
 value : loop-segments/s with the ensemble resident in HBM (wl_eval_device,
         CUDA events on the library's stream; 160 MiB ensemble > L2).
-e2e   : the same metric through wl_ensemble_upload + wl_eval + release with
+e2e   : the same metric through wl_ensemble_upload + wl_tint + release with
         host buffers (host->device copy of the ensemble and instances, and
-        device->host copy of every group result inside the timed region).
+        device->host copy of the effective action densities inside the timed
+        region).
+accuracy : the FP64 oracle on a seeded sample of the timed instances.
+batch : the uneven-batch configuration (16 jobs by default) in one
+        persistent graph launch, against the plain per-instance kernel and
+        the library's own per-instance path.
+serve : the served-stream configuration's request mix through the server
+        (100 requests per phase by default).
 --impl reference : the reference's Wilson-loop formula as C (the FP32 port
         of intEV.cu:408-571 + Integrand.c:325-407) on all host cores, on a
         bounded sample of the same workload.
@@ -47,12 +54,23 @@ FLUX = [0.1, 1.0, 10.0]
 NINT = 4
 GROUP = 128
 # Algorithmic FP32 and MUFU operations per loop-segment of smooth spinor QED
-# at 5 Simpson nodes (fixed, not tuned): segment set-up ~25 FP32 (scale and
-# shift 4, a/b/c 6, cross term 2, clamps 4, Simpson combine 3, compensated
-# sums 8); per node 4 FP32 + 1 MUFU reciprocal (f/rho^2 = 1/(l2 + rho^2)) and
-# 2 FP32 for the spin part: 25 + 5 x 6 = 55 FP32, 5 MUFU.
-ALG_FP32_PER_SEG = 55
+# at 5 Simpson nodes (fixed, not tuned).  MUFU: 5 reciprocals (f/rho^2 =
+# 1/(l2 + rho^2) at the two ends and three interior nodes; f' = l2 (f/rho^2)^2
+# needs none).  FP32: 38, the FP32 operations the kernel executes per
+# segment (ncu instruction mix: FFMA 21.2 + FADD 11.9 + FMUL 5.1): per
+# interior node 2 FMAs for rho^2, a square and 2 sums (15 for three nodes),
+# and the segment's set-up (point scaling, a, b, c, the cross term, the
+# polynomial's constants, the end squares, the Simpson combines); the clamps
+# run on the integer pipe.  No formulation with fewer is known here.
+ALG_FP32_PER_SEG = 38
 ALG_MUFU_PER_SEG = 5
+# MUFU operations per loop-segment (lattice: per segment-image) of the
+# profiles of the uneven batch at 5 nodes: smooth 1 reciprocal per node;
+# Gaussian 1 ex2 + 1 reciprocal per node (the large-x branch; both branches
+# are evaluated); the lattice's Gaussian image integrand the same per image
+ALG_MUFU_BY_PROFILE = {"smooth": 5, "gaussian": 10, "lattice": 10}
+# MUFU reciprocal issue rate of one SM per clock (Blackwell SFU: 16 lanes)
+MUFU_PER_SM_CLK = 16
 # loop data a segment reads (one float4 point) -- HBM side of the roofline
 ALG_BYTES_PER_POINT = 16
 
@@ -147,7 +165,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_sample(seconds_target=12.0, threads=0):
+def cpu_sample(seconds_target=12.0, threads=0, with_fraction=False):
     """The FP32 C port of the reference's per-loop formula and EVMean on all
     host cores, timed on a bounded sample of the workload."""
     from oracle import oracle
@@ -175,8 +193,36 @@ def cpu_sample(seconds_target=12.0, threads=0):
     dt = time.perf_counter() - t0
     segs = n * nl * PPL
     cores = threads if threads > 0 else (os.cpu_count() or 1)
-    return segs / dt, cores, "%d loops x %d points x %d (rho,T) instances (3 F each), %.1f s" % (
-        nl, PPL, n, dt)
+    desc = "%d loops x %d points x %d (rho,T) instances (3 F each), %.1f s" % (nl, PPL, n, dt)
+    if with_fraction:
+        return segs / dt, cores, desc, segs / float(NL * PPL * NT * NRHO)
+    return segs / dt, cores, desc
+
+
+def accuracy_check(loops, groups, cx, cy, T, n=32, seed=0):
+    """The FP64 oracle (the checker) on a seeded sample of n timed instances,
+    all three F, against the per-group <W> the GPU wrote in the timed region:
+    the error as oracle.accuracy states it (relative error with its floor,
+    the strict region, and the error of the mean in units of the Monte Carlo
+    error bar)."""
+    from oracle import oracle
+
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(len(T), n, replace=False))
+    # the instance the FP32 kernel evaluates: float(cx), float(cy), float(sqrt T)^2
+    rt = np.sqrt(T[idx]).astype(np.float32).astype(np.float64)
+    ox = np.asarray(cx[idx], np.float32).astype(np.float64)
+    oy = np.asarray(cy[idx], np.float32).astype(np.float64)
+    t0 = time.perf_counter()
+    ref, S = oracle.eval_groups(loops, ox, oy, rt * rt, FLUX,
+                                oracle.field("smooth", fermion=1, nint=NINT), return_scale=True)
+    acc = oracle.accuracy(groups[idx], ref, S, FLUX, rt * rt)
+    out = {k: v for k, v in acc.items() if not isinstance(v, np.ndarray)}
+    out.update({"sample": "%d seeded instances of the timed step (every F), full ensemble"
+                          % n, "oracle_seconds": time.perf_counter() - t0,
+                "sentinel_loops": "none: the largest cosh argument of this workload is ~220 "
+                                  "(the reference's sentinel needs > 600)"})
+    return out
 
 
 def run_reference(args, world, rank):
@@ -187,15 +233,18 @@ def run_reference(args, world, rank):
         cpu_sample(seconds_target=2.0)
     info = None
     for _ in range(args.steps):
-        v, cores, sample = cpu_sample(seconds_target=args.cpu_seconds)
+        v, cores, sample, frac = cpu_sample(seconds_target=args.cpu_seconds, with_fraction=True)
         vals.append(v)
-        info = (cores, sample)
+        info = (cores, sample, frac)
     value = float(np.median(vals))
     segs_step = NL * PPL * NT * NRHO
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "segments/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": segs_step / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        # each step times a bounded sample of the workload; ms_per_step is the
+        # full step at the sampled rate (the work is linear in loops x instances)
+        "ms_per_step": segs_step / value * 1e3, "ms_per_step_extrapolated": True,
+        "sample_fraction": info[2], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config_dict(),
         "cpu_baseline": {"value": value, "unit": "segments/s", "cores": info[0], "kind": "port",
@@ -245,51 +294,130 @@ def c4_jobs(wltube, ctx, njobs, seed=4, profiles=("smooth", "gaussian")):
     return jobs, ens
 
 
+def job_images_per_segment(ctx, job, stride=16):
+    """Mean lattice images per loop-segment of a lattice job (the kernel's
+    selection, on every stride-th instance); 1 for the single-tube profiles."""
+    if job["profile"] != "lattice":
+        return 1.0
+    host = ctx.download(job["handle"])
+    bbox = np.stack([host[:, :, 0].min(1), host[:, :, 0].max(1),
+                     host[:, :, 1].min(1), host[:, :, 1].max(1)], axis=1)
+    f = job["field"]
+    lam = float(np.sqrt(f.lambda2))
+    sl = slice(0, None, stride)
+    imgs = lattice_image_counts(bbox, job["cx"][sl], job["cy"][sl], job["T"][sl], f.tubedist,
+                                lam, f.rimage)
+    return float(imgs.mean()) / host.shape[0]
+
+
+def single_instance_ms(ctx, job, idx):
+    """Device time of the library's own per-instance path: one wl_eval_device
+    per instance (a single instance runs on the loop-parallel kernel: one
+    warp per loop, instance setup + sweep + group reduction, three launches),
+    CUDA events on the context's stream around each call."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    d = lambda a: torch.tensor(np.atleast_1d(a), dtype=torch.float64, device="cuda")  # noqa
+    total = 0.0
+    for i in idx:
+        cx, cy, T = d(job["cx"][i]), d(job["cy"][i]), d(job["T"][i])
+        dm = torch.empty(len(job["F"]), dtype=torch.float64, device="cuda")
+        ds = torch.empty_like(dm)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.eval_device(job["handle"], job["field"], 1, cx.data_ptr(), cy.data_ptr(),
+                        T.data_ptr(), job["F"], job["group"], 0, dm.data_ptr(), ds.data_ptr())
+        e1.record(stream)
+        ctx.synchronize()
+        total += e0.elapsed_time(e1)
+    return total
+
+
+def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
+                  mufu_peak=None):
+    """The uneven-batch configuration (seed 4): njobs jobs drawn from its
+    distribution, autotuned, evaluated in one persistent graph-captured launch
+    per step; against two per-instance denominators on per_job_sample
+    instances of every job: the plain kernel (one thread per loop walking its
+    points from global memory, the reference kernel's structure) and the
+    library's own single-instance path (wl_eval_device per instance)."""
+    jobs, ens = c4_jobs(wltube, ctx, njobs, profiles=profiles)
+    total = sum(j["segments"] for j in jobs)
+    sample = [dict(j, cx=j["cx"][::8], cy=j["cy"][::8], T=j["T"][::8]) for j in jobs[:8]]
+    t_tune = time.perf_counter()
+    pts, ctas = ctx.batch_autotune(sample)
+    t_tune = time.perf_counter() - t_tune
+    for _ in range(warmup):
+        ctx.batch_eval(jobs, graph=True)
+    ms = []
+    for _ in range(steps):
+        ctx.batch_eval(jobs, graph=True)
+        ms.append(ctx.batch_stats()["device_ms"])
+    st = ctx.batch_stats()
+    bms = float(np.median(ms))
+    batched = total / (bms * 1e-3)
+    # the per-instance denominators on the same sample of every job
+    psegs, pms, sms, pinst = 0, 0.0, 0.0, 0
+    for j in jobs:
+        n = len(j["T"])
+        idx = np.unique(np.linspace(0, n - 1, min(per_job_sample, n)).astype(int))
+        _, _, _, t = ctx.eval_plain(j["handle"], j["field"], j["cx"][idx], j["cy"][idx],
+                                    j["T"][idx], j["F"], j["group"])
+        pms += t
+        sms += single_instance_ms(ctx, j, idx)
+        psegs += j["segments"] // n * len(idx)
+        pinst += len(idx)
+    plain = psegs / (pms * 1e-3)
+    single = psegs / (sms * 1e-3)
+    out = {
+        "metric": "loop-segments/s (uneven batch, one persistent graph launch)",
+        "value": batched, "unit": "segments/s", "ms_per_step": bms, "steps": steps,
+        "warmup": warmup, "jobs": len(jobs), "segments_per_step": int(total),
+        "tiles": st["tiles"], "grid": st["grid"],
+        "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas, "seconds": t_tune},
+        "plain_per_instance": {"value": plain, "unit": "segments/s", "device_ms": pms,
+                               "sample_instances": pinst,
+                               "kernel": "plain_kernel: one thread per loop, points read "
+                                         "from global memory (the reference kernel's "
+                                         "structure), one launch per instance"},
+        "library_per_instance": {"value": single, "unit": "segments/s", "device_ms": sms,
+                                 "sample_instances": pinst,
+                                 "path": "wl_eval_device with one instance per call "
+                                         "(loop-parallel kernel + reduction)"},
+        "speedup_vs_plain": batched / plain,
+        "speedup_vs_library_per_instance": batched / single,
+        "config": {"workload": "uneven batch drawn as the 512-instance configuration "
+                               "(seed 4), %d jobs, profiles %s, spinor, 5 Simpson nodes, "
+                               "F and lambda log-uniform, ppl 512-8192, Nl 1024-8192, "
+                               "16-256 T x 4-64 rho per job" % (len(jobs), "+".join(profiles)),
+                   "ensembles": len(ens)},
+    }
+    if mufu_peak:
+        mufu = 0.0
+        for j in jobs:
+            mufu += j["segments"] * ALG_MUFU_BY_PROFILE[j["profile"]] * \
+                job_images_per_segment(ctx, j)
+        out["roofline"] = {"bound": "mufu", "achieved_gops": mufu / (bms * 1e-3) / 1e9,
+                           "peak_gops": mufu_peak / 1e9,
+                           "frac": mufu / (bms * 1e-3) / mufu_peak,
+                           "alg_mufu_per_segment": ALG_MUFU_BY_PROFILE,
+                           "note": "lattice jobs count their selected images per segment"}
+    for h in ens.values():
+        ctx.release(h)
+    return out
+
+
 def run_batch(args):
-    """Uneven batch in one persistent graph-captured launch vs the plain
-    per-instance kernel (one launch per instance) on a sample."""
+    """Uneven batch in one persistent graph-captured launch vs the per-instance
+    paths on a sample (one JSON line)."""
     import wltube
 
     ctx = wltube.Context(0)
     profiles = tuple(args.batch_profiles.split(","))
-    jobs, ens = c4_jobs(wltube, ctx, args.jobs, profiles=profiles)
-    total = sum(j["segments"] for j in jobs)
-    # autotune on a sample: the first jobs with every 8th instance
-    sample = [dict(j, cx=j["cx"][::8], cy=j["cy"][::8], T=j["T"][::8]) for j in jobs[:8]]
-    pts, ctas = ctx.batch_autotune(sample)
-    for _ in range(args.warmup):
-        ctx.batch_eval(jobs, graph=True)
-    ms = []
-    for _ in range(args.steps):
-        ctx.batch_eval(jobs, graph=True)
-        ms.append(ctx.batch_stats()["device_ms"])
-    st = ctx.batch_stats()
-    batched = total / (np.median(ms) * 1e-3)
-    # plain per-instance kernel on a sample of instances of every job
-    psegs, pms, pinst = 0, 0.0, 0
-    for j in jobs:
-        idx = np.linspace(0, len(j["T"]) - 1, 2).astype(int)
-        _, _, _, t = ctx.eval_plain(j["handle"], j["field"], j["cx"][idx], j["cy"][idx],
-                                    j["T"][idx], j["F"], j["group"])
-        Nl_ppl = j["segments"] // len(j["T"])
-        psegs += Nl_ppl * len(idx)
-        pinst += len(idx)
-        pms += t
-    plain = psegs / (pms * 1e-3)
-    print(json.dumps({
-        "metric": "loop-segments/s (uneven batch, one persistent graph launch)",
-        "value": batched, "unit": "segments/s", "ms_per_step": float(np.median(ms)),
-        "steps": args.steps, "warmup": args.warmup, "jobs": len(jobs),
-        "segments_per_step": int(total), "tiles": st["tiles"], "grid": st["grid"],
-        "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas},
-        "plain_per_instance": {"value": plain, "unit": "segments/s",
-                               "sample_instances": pinst, "device_ms": pms,
-                               "jobs": len(jobs)},
-        "speedup_vs_plain": batched / plain,
-        "config": {"workload": "uneven batch drawn as the 512-instance configuration "
-                               "(seed 4), %d jobs, profiles %s, spinor, "
-                               "5 Simpson nodes" % (len(jobs), "+".join(profiles)),
-                   "ensembles": len(ens)}}))
+    out = batch_measure(ctx, wltube, args.jobs, profiles, args.steps, args.warmup,
+                        mufu_peak=ctx.peak_probe(1))
+    print(json.dumps(out))
     ctx.close()
 
 
@@ -360,21 +488,22 @@ def serve_phase(wltube, reqs, rate, seed, max_requests):
     return st
 
 
-def run_serve(args):
-    """Served stream: an overload phase (Poisson arrivals at the configuration's
-    lowest rate, 200 req/s) measures the sustained throughput; a second phase
-    offers 70% of that rate and reports the latency percentiles."""
+def serve_measure(n, profiles, max_requests, overload_rate=200.0, load=0.7):
+    """Served stream drawn as the served-stream configuration (seed 5): an
+    overload phase (Poisson arrivals at overload_rate req/s, the
+    configuration's lowest rate) measures the sustained throughput; a second
+    phase offers `load` of that rate and gives the latency percentiles.
+    Returns the sub-object of the bench line."""
     import wltube
 
-    n = args.requests
-    profiles = tuple(args.serve_profiles.split(","))
     reqs = c5_requests(wltube, 2 * n, profiles=profiles)
     phases = []
-    for name, rate, part in (("overload", 200.0, reqs[:n]), ("sustainable", None, reqs[n:])):
+    for name, rate, part in (("overload", overload_rate, reqs[:n]),
+                             ("sustainable", None, reqs[n:])):
         if rate is None:
-            rate = 0.7 * phases[0]["sustained_req_s"]
+            rate = load * phases[0]["sustained_req_s"]
         t0 = time.time()
-        st = serve_phase(wltube, part, rate, 50 + len(phases), args.max_requests)
+        st = serve_phase(wltube, part, rate, 50 + len(phases), max_requests)
         sys.stderr.write("serve phase %s: %.1f s, %s\n" % (name, time.time() - t0, st))
         wall = st["wall_s"]  # first submit -> last completion of the phase
         phases.append({"phase": name, "offered_req_s": rate, "requests": len(part),
@@ -382,22 +511,37 @@ def run_serve(args):
                        "failed": st["failed"],
                        "sustained_req_s": st["completed"] / wall if wall > 0 else None,
                        "segments_per_s": st["segments"] / wall if wall > 0 else None,
-                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "p999_ms": st["p999_ms"],
+                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                       "p999_ms": st["p999_ms"] if len(part) >= 1000 else None,
                        "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
-                       "launches": st["launches"], "resident_ensembles": st["resident_ensembles"]})
+                       "launches": st["launches"],
+                       "device_busy_frac": st["device_busy_s"] / wall if wall > 0 else None,
+                       "device_busy_in_span": (st["device_busy_s"] / st["device_span_s"]
+                                               if st["device_span_s"] > 0 else None),
+                       "resident_ensembles": st["resident_ensembles"]})
     sus = phases[1]
-    print(json.dumps({
+    return {
         "metric": "serve p50/p99 latency and loop-segments/s (continuous batching)",
         "value": sus["segments_per_s"], "unit": "segments/s",
         "p50_ms": sus["p50_ms"], "p99_ms": sus["p99_ms"], "p999_ms": sus["p999_ms"],
+        "p999_note": "p99.9 is reported from 1000 requests per phase up (below that it "
+                     "is the maximum)",
+        "sustained_req_s": phases[0]["sustained_req_s"],
         "phases": phases,
         "config": {"workload": "served stream drawn as the served-stream configuration "
                                "(seed 5): %d requests per phase, profiles %s, spinor, "
                                "5 Simpson nodes, half <W> and half effective-action-density "
-                               "requests, ensembles resident before the phase"
-                               % (n, "+".join(profiles)),
-                   "max_requests": args.max_requests, "quantum_ms": 20.0,
-                   "points_per_tile": 16384}}))
+                               "requests, ensembles resident before the phase; the "
+                               "configuration's 20000 requests at its sustained rate would "
+                               "take hours of device time" % (n, "+".join(profiles)),
+                   "max_requests": max_requests, "quantum_ms": 20.0,
+                   "points_per_tile": 16384}}
+
+
+def run_serve(args):
+    """Served stream through the request server (one JSON line)."""
+    print(json.dumps(serve_measure(args.requests, tuple(args.serve_profiles.split(",")),
+                                   args.max_requests)))
 
 
 # Algorithmic MUFU operations per segment-image of the lattice (5 nodes of the
@@ -514,13 +658,17 @@ def run_lattice(args):
 
 
 def effact_legacy(ctx, h, Nl, ppl, l2, F, nrho, panels):
-    """The same effective action through the reference's own caller chain,
-    relinked against this library and otherwise unchanged: for every radial
-    node of EAction's rule (EffAct.c:258-306) rhogrand's integrateT(40, p)
-    (EffAct.c:15-40) -> Tfunc -> EV() with a struct Wparams of device buffers
-    (EffAct.c:368-413), EV at the reference's 50 intervals; then the same
-    radial sum.  Returns its time, action and EV() calls.  The Leffvsrho
-    lines integrateT prints go to /dev/null."""
+    """The same effective action through the reference's caller chain as this
+    repository restates it in C (host/wl_host.c, libwlhost.so: integrateT ->
+    Tfunc -> EV with the reference's signatures; the reference's own Tint.c
+    and Integrand.c link against libwlgpu.so the same way, which
+    tests/test_reference_host_link.py checks, but are not compiled on the
+    GPU host): for every radial node of EAction's rule (EffAct.c:258-306)
+    rhogrand's integrateT(40, p) (EffAct.c:15-40) -> Tfunc -> EV() with a
+    struct Wparams of device buffers (EffAct.c:368-413), EV at the
+    reference's 50 intervals; then the same radial sum.  Returns its time,
+    action and EV() calls.  The Leffvsrho lines integrateT prints go to
+    /dev/null."""
     import ctypes as C
 
     import torch
@@ -565,8 +713,8 @@ def effact_legacy(ctx, h, Nl, ppl, l2, F, nrho, panels):
     groups = -1.0 / (2 * np.pi) * np.einsum("r,r,rg->g", w, rho, np.where(np.isinf(I), 0.0, I))
     return {"value": sec, "unit": "s", "effective_action": float(groups.mean()),
             "standard_error": float(groups.std(ddof=1) / np.sqrt(len(groups))),
-            "path": "integrateT -> Tfunc -> EV (libwlhost.so, libwlgpu.so), one call per "
-                    "radial node"}
+            "path": "integrateT -> Tfunc -> EV (the C restatement of Tint.c / Integrand.c "
+                    "in libwlhost.so, on libwlgpu.so), one call per radial node"}
 
 
 def run_effact(args):
@@ -626,15 +774,21 @@ def main():
                     help="profiles of the batch jobs (the configuration's mix: smooth, "
                          "gaussian and lattice a = 5 lambda)")
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
+    ap.add_argument("--accuracy-instances", type=int, default=32,
+                    help="timed instances the FP64 oracle checks (default line)")
+    ap.add_argument("--batch-jobs", type=int, default=16,
+                    help="jobs of the default line's uneven-batch sub-object (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=100,
+                    help="requests per phase of the default line's serve sub-object (0: skip)")
     ap.add_argument("--lattice-grid", type=int, default=32,
                     help="centres per side of the unit cell (lattice workload)")
     ap.add_argument("--lattice-tstride", type=int, default=12,
                     help="take every n-th of the 96 proper times (lattice workload)")
     ap.add_argument("--lattice-cases", default="2:0,2:1,5:0,5:1,10:0,10:1",
                     help="a:fermion pairs of the lattice workload")
-    ap.add_argument("--serve-profiles", default="smooth,gaussian",
-                    help="profiles of the served requests (lattice requests cost up to "
-                         "hundreds of single-tube segments each: one per image)")
+    ap.add_argument("--serve-profiles", default="smooth,gaussian,lattice",
+                    help="profiles of the served requests (the configuration's mix: smooth, "
+                         "gaussian and lattice a = 5 lambda)")
     ap.add_argument("--max-requests", type=int, default=64,
                     help="requests the server admits at once (serve workload)")
     args = ap.parse_args()
@@ -758,13 +912,29 @@ def main():
                         "F": FLUX[1],
                         "L_eff": [float(leff[0, 1]), float(leff[len(rho) // 8, 1])],
                         "jackknife_err": [float(lerr[0, 1]), float(lerr[len(rho) // 8, 1])]}
-    cpu = None
+    cpu = acc = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        # the CPU legs: the FP32 port timed on the host cores, and the FP64
+        # oracle checking a sample of what the timed steps wrote
         v, cores, sample = cpu_sample(seconds_target=args.cpu_seconds)
         cpu = {"value": v, "unit": "segments/s", "cores": cores, "kind": "port",
                "sample": sample}
+        groups = dgrp.cpu().numpy().reshape(ninst, len(FLUX), ng)
+        acc = accuracy_check(ctx.download(h), groups, cx, cy, T, n=args.accuracy_instances)
+    batch = serve = None
+    if rank == 0 and world == 1 and not args.small:
+        if args.batch_jobs > 0:
+            batch = batch_measure(ctx, wltube, args.batch_jobs,
+                                  tuple(args.batch_profiles.split(",")), steps=1, warmup=1,
+                                  mufu_peak=mufu_peak)
+        if args.serve_requests > 0:
+            serve = serve_measure(args.serve_requests, tuple(args.serve_profiles.split(",")),
+                                  args.max_requests)
     if rank != 0:
         return
+    props = torch.cuda.get_device_properties(local)
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    nominal = MUFU_PER_SM_CLK * props.multi_processor_count * sm_mhz * 1e6
     line = {
         "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -773,15 +943,19 @@ def main():
         "config": config_dict(),
         "W_evals_per_s": world * ninst * len(FLUX) / (ms_step * 1e-3),
         # the binding pipe is the MUFU (5 reciprocals per segment, exact for
-        # the formula; 16 per SM per clock); the FP32 side is reported beside
-        # it against the scope table's algorithmic count of 55, which the
-        # packed-pair kernel undercuts (38 FP32 operations per segment)
+        # the formula; 16 per SM per clock); the FP32 pipe is reported beside
+        # it with the 38 operations per segment the kernel executes
         "roofline": {
             "bound": "mufu", "unit": "Gop/s",
             "achieved": mufu_ach / 1e9, "peak": mufu_peak / 1e9, "frac": mufu_ach / mufu_peak,
             "traffic": traffic,
             "peak_source": "MUFU rcp.approx probe measured in this run (MEASURED_PEAKS.json "
                            "has no MUFU or FP32 figure)",
+            "sm_count": props.multi_processor_count,
+            "nominal_peak": nominal / 1e9,
+            "nominal_source": "16 MUFU reciprocals per SM per clock x SMs x the median SM "
+                              "clock sampled during the timed region",
+            "probe_vs_nominal": mufu_peak / nominal,
             "alg_ops_per_segment": {"fp32": ALG_FP32_PER_SEG, "mufu": ALG_MUFU_PER_SEG},
             "fp32": {"achieved": fp32_ach / 1e9, "peak": fp32_peak / 1e9,
                      "frac": fp32_ach / fp32_peak,
@@ -789,9 +963,17 @@ def main():
             "hbm": {"achieved_gbs": hbm_ach, "peak_gbs": hbm_peak,
                     "frac": hbm_ach / hbm_peak if hbm_peak else None,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+            "traffic_vs_algorithmic": (traffic / (NL * PPL * ALG_BYTES_PER_POINT)
+                                       if traffic else None),
+            "traffic_note": "ncu DRAM bytes per launch: the ensemble read once (167.8 MB, the "
+                            "algorithmic bytes) plus the FP64 partial sums [chunk][F][3]"
+                            "[instance] written for the group reduction (377 MB); HBM is at "
+                            "~0.02 % of its peak, so neither bounds the kernel",
             "kernel_ms": per_launch_ms,
         },
+        "accuracy": acc,
         "e2e": e2e, "L_eff_sample": leff_summary, "cpu_baseline": cpu,
+        "batch": batch, "serve": serve,
         "gpu_launches": launches, "clocks": clk,
     }
     print(json.dumps(line))

@@ -365,6 +365,10 @@ typedef struct {
   long long launches;       /* persistent-kernel launches                     */
   int resident_ensembles;
   double hbm_bytes_in_use;  /* ensembles + admitted requests' buffers         */
+  double device_busy_s;     /* union of the launches' device intervals (the
+                               persistent kernel and the heavy-profile sweeps,
+                               event to event) since the statistics were reset */
+  double device_span_s;     /* first launch start -> last launch end, same clock */
 } wl_server_stats;
 
 typedef struct wl_server wl_server;

@@ -49,7 +49,7 @@ __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, 
                                             consumed);
         break;
       case kLattice:
-        if constexpr (NINT == 4) sweep_tile<kLattice, FERM, NINT>(A, tx, chunk, S, consumed);
+        if constexpr (NINT == 4) sweep_tile_lat<FERM>(A, tx, chunk, S, consumed);
         break;
       default: break;
     }

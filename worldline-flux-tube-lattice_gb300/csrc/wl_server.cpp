@@ -145,6 +145,11 @@ struct wl_server {
   cudaEvent_t adm_ev = nullptr;
   long long adm_seq = 0, waited_seq[2] = {0, 0};
   cudaEvent_t ev_start[2] = {nullptr, nullptr}, ev_stop[2] = {nullptr, nullptr};
+  // device clock of the statistics: recorded before the first launch after a
+  // reset; each retired launch adds its [start, stop] in ms from it
+  cudaEvent_t ev_base = nullptr;
+  bool base_recorded = false, base_reset = false;  // base_reset: under mu
+  std::vector<std::pair<double, double>> spans;    // under mu
   bool busy[2] = {false, false};
   double busy_work[2] = {0.0, 0.0};
   int busy_tiles[2] = {0, 0};
@@ -641,6 +646,18 @@ void launch_quantum(wl_server *s, int k) {
        "tile upload");
     ck(cudaMemsetAsync(s->d_counter + k, 0, sizeof(int), st), "counter reset");
   }
+  {
+    bool reset;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      reset = s->base_reset;
+      s->base_reset = false;
+    }
+    if (reset || !s->base_recorded) {
+      ck(cudaEventRecord(s->ev_base, st), "event");
+      s->base_recorded = true;
+    }
+  }
   ck(cudaEventRecord(s->ev_start[k], st), "event");
   if (n > 0) {
     wl::BatchArgs B;
@@ -699,6 +716,16 @@ bool retire_launches(wl_server *s) {
     progress = true;
     float ms = 0.0f;
     ck(cudaEventElapsedTime(&ms, s->ev_start[k], s->ev_stop[k]), "elapsed");
+    float t0 = 0.0f, t1 = 0.0f;
+    if (cudaEventElapsedTime(&t0, s->ev_base, s->ev_start[k]) == cudaSuccess &&
+        cudaEventElapsedTime(&t1, s->ev_base, s->ev_stop[k]) == cudaSuccess) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      // a launch issued before the base was re-recorded (t0 < 0) belongs to
+      // the previous statistics
+      if (!s->base_reset && t0 >= 0.0f) s->spans.emplace_back((double)t0, (double)t1);
+    } else {
+      cudaGetLastError();  // a launch started before the base was re-recorded
+    }
     // a launch that filled every CTA slot measures the device rate
     if (s->busy_tiles[k] >= s->grid_max && ms > 0.05f) {
       const double r = s->busy_work[k] / ms;
@@ -873,6 +900,7 @@ int wl_server_create(const wl_server_config *cfg, wl_server **out) {
     e = cudaStreamCreateWithFlags(&s->st[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev_start[k]);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev_stop[k]);
+    if (e == cudaSuccess && !s->ev_base) e = cudaEventCreate(&s->ev_base);
     if (e == cudaSuccess) e = cudaMalloc((void **)&s->d_tiles[k], sizeof(wl::BatchTile) * kMaxQuantumTiles);
     if (e == cudaSuccess)
       e = cudaHostAlloc((void **)&s->h_tiles[k], sizeof(wl::BatchTile) * kMaxQuantumTiles,
@@ -970,6 +998,24 @@ int wl_server_get_stats(wl_server *srv, wl_server_stats *out) {
   out->launches = srv->n_launch;
   out->resident_ensembles = srv->pub_resident;
   out->hbm_bytes_in_use = srv->pub_in_use;
+  // union of the launch intervals (two streams may overlap)
+  std::vector<std::pair<double, double>> sp = srv->spans;
+  std::sort(sp.begin(), sp.end());
+  double busy = 0.0, lo = 0.0, hi = -1.0;
+  for (const auto &x : sp) {
+    if (x.first > hi) {
+      if (hi > lo) busy += hi - lo;
+      lo = x.first;
+      hi = x.second;
+    } else {
+      hi = std::max(hi, x.second);
+    }
+  }
+  if (hi > lo) busy += hi - lo;
+  out->device_busy_s = busy * 1e-3;
+  double last = 0.0;
+  for (const auto &x : sp) last = std::max(last, x.second);
+  out->device_span_s = sp.empty() ? 0.0 : (last - sp.front().first) * 1e-3;
   return WL_OK;
 }
 
@@ -979,6 +1025,8 @@ int wl_server_reset_stats(wl_server *srv) {
   srv->n_sub = srv->n_done = srv->n_rej = srv->n_fail = srv->n_launch = 0;
   srv->lat_ms.clear();
   srv->seg_done = 0.0;
+  srv->spans.clear();
+  srv->base_reset = true;
   return WL_OK;
 }
 
@@ -1020,6 +1068,7 @@ int wl_server_destroy(wl_server *srv) {
     cudaFree(kv.second.second);
   }
   if (srv->adm_ev) cudaEventDestroy(srv->adm_ev);
+  if (srv->ev_base) cudaEventDestroy(srv->ev_base);
   if (srv->d_counter) cudaFree(srv->d_counter);
   if (srv->d_slots) cudaFree(srv->d_slots);
   if (srv->cs) cudaStreamDestroy(srv->cs);

@@ -208,6 +208,251 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
   return true;
 }
 
+// ------------------------------------------------ lattice, images outer --
+// One segment u_i -> u_j for two images at once (packed pair; u = the loop
+// point minus the image centre R, scaled): the Gaussian tube's Simpson
+// integral in units of x = rho^2 / lambda^2 (exact mode), each half as
+// segment_lattice evaluates one image.  Adds cross * S to ph and the spin
+// integral to sp (its 1/l2 scale is applied per loop).
+template <bool FERM>
+__device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, float2 ujy,
+                                         float2 il2, float2 &ph, float2 &sp) {
+  const float2 dx = add2(ujx, neg2(uix)), dy = add2(ujy, neg2(uiy));
+  const float2 as = mul2(fma2(uix, uix, mul2(uiy, uiy)), il2);
+  const float2 bs2 = mul2(mul2(f2(2.0f), fma2(uix, dx, mul2(uiy, dy))), il2);
+  const float2 cs = mul2(fma2(dx, dx, mul2(dy, dy)), il2);
+  const float2 cross = mul2(fma2(uix, dy, neg2(mul2(uiy, dx))), il2);
+  float2 q0, e0, q1, e1;
+  gauss_q2(as, q0, e0);
+  gauss_q2(add2(add2(as, bs2), cs), q1, e1);
+  float2 so = f2(0.f), se = f2(0.f), fo = f2(0.f), fe = f2(0.f);
+#pragma unroll
+  for (int j = 1; j < 4; j++) {
+    const float t = (float)j * 0.25f;
+    float2 q, e;
+    gauss_q2(fma2(fma2(cs, f2(t), bs2), f2(t), as), q, e);
+    if (j & 1) {
+      so = add2(so, q);
+      if (FERM) fo = add2(fo, e);
+    } else {
+      se = add2(se, q);
+      if (FERM) fe = add2(fe, e);
+    }
+  }
+  ph = fma2(cross, fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(q0, q1))), ph);
+  if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(e0, e1))));
+}
+
+// the rarely taken opening / closing segments as one called copy
+template <bool FERM>
+__device__ __noinline__ float4 lat_seg2_called(float2 uix, float2 uiy, float2 ujx, float2 ujy,
+                                               float2 il2, float4 acc) {
+  float2 ph = make_float2(acc.x, acc.y), sp = make_float2(acc.z, acc.w);
+  lat_seg2<FERM>(uix, uiy, ujx, ujy, il2, ph, sp);
+  return make_float4(ph.x, ph.y, sp.x, sp.y);
+}
+
+// Lattice tile at 4 intervals with the images outer: one instance per
+// thread; for every staged chunk of a loop, each pair of the (loop,
+// instance)'s images walks all of the chunk's segments.  A loop point minus
+// an image centre is image-independent up to the shift, so the walk's state
+// between chunks is the raw unit-loop points; per image pair the walk is
+// uniform across the warp (no per-segment image loop, no row logic) and every
+// FP32 operation is a packed pair.  The images of a (loop, instance) are its
+// range of image_range() flattened row by row (k -> m0 + k / w, n0 + k % w),
+// taken two at a time; an odd last image and images outside the |R| disk
+// are computed and not added.  Sums: per image pair, blocks of 8 groups in
+// FP32, each half added in image order to the loop's Kahan-compensated
+// totals.  The order depends only on the (loop, instance), so results do
+// not depend on the tile's other instances.
+template <bool FERM>
+__device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, int chunk,
+                                               const SweepShared &S, int &consumed) {
+  const int tid = threadIdx.x;
+  const int slot = tile_x * kSweepThreads + tid;
+  const bool live = slot < A.ninst;
+  const int sl = live ? slot : A.ninst - 1;
+  const int ic = A.perm ? A.perm[sl] : sl;
+  const int l0 = chunk * A.chunk_loops;
+  const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
+  const int K = A.chunk_loops * nck;
+  float4 *const ring = S.ring;
+  uint64_t *const full_bar = S.full_bar;
+  const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic];
+  const FieldDev &F = A.field;
+  const df tq = {A.tqh[ic], A.tql[ic]};
+  const int base = consumed;
+
+  auto issue = [&](int k) {
+    const int st = (base + k) % kSweepStages;
+    const int l = l0 + k / nck, c = k % nck;
+    const int p0 = c * kSweepChunkPts;
+    const int np = min(kSweepChunkPts, A.ppl - p0);
+    const uint32_t bytes = (uint32_t)np * (uint32_t)sizeof(float4);
+    mbar_arrive_expect_tx(&full_bar[st], bytes);
+    bulk_g2s(ring + st * kSweepChunkPts, A.loops + (size_t)l * A.ppl + p0, bytes, &full_bar[st]);
+  };
+  if (tid == 0)
+    for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
+#pragma unroll
+  for (int r = 0; r < kMaxF * 3; ++r) S.sacc[r][tid] = 0.0;
+
+  const float2 s2 = f2(s), il2 = f2(F.inv_l2);
+  float ph[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
+  float sp[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
+  // raw unit-loop points: the loop's first three and the sub-loops' last ones
+  float2 w0 = f2(0.f), w1 = f2(0.f), w2 = f2(0.f), w3 = f2(0.f);
+  float2 wA = f2(0.f), wB = f2(0.f), wO = f2(0.f);
+  ImgRange img = {0, -1, 0, -1, 1};
+  int nimg = 0, width = 1;
+
+  int k = 0;
+  for (; k < K; ++k) {
+    const int st = (base + k) % kSweepStages;
+    const uint32_t par = (uint32_t)((base + k) / kSweepStages) & 1u;
+    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) *S.bad = 1;
+    const int c = k % nck;
+    const int p0 = c * kSweepChunkPts;
+    const int p1 = min(A.ppl, p0 + kSweepChunkPts);
+    const float2 *pts = reinterpret_cast<const float2 *>(ring + st * kSweepChunkPts);
+    auto raw = [&](int p) { return pts[2 * (p - p0)]; };
+    if (c == 0) {
+#pragma unroll
+      for (int r = 0; r < 3; ++r) ph[r] = pc[r] = sp[r] = sc[r] = 0.f;
+      img = image_range(A.bbox[l0 + k / nck], s, cx, cy, F);
+      width = max(img.n1 - img.n0 + 1, 1);
+      nimg = (img.m1 >= img.m0 && img.n1 >= img.n0) ? (img.m1 - img.m0 + 1) * width : 0;
+      w0 = raw(0);
+      w1 = raw(1);
+      w2 = raw(2);
+      w3 = raw(3);
+      wA = w0;
+      wB = w2;
+      wO = w3;
+    }
+    const bool last = c == nck - 1;
+    const int qa = c == 0 ? 1 : (p0 >> 2), qend = p1 >> 2;
+    for (int i = 0; i < nimg; i += 2) {
+      // the pair's images and whether each counts (exists, inside the disk)
+      const int ma = img.m0 + i / width, na = img.n0 + i % width;
+      const int ib = min(i + 1, nimg - 1);
+      const int mb = img.m0 + ib / width, nb = img.n0 + ib % width;
+      const bool okA = img.inside || (float)(ma * ma) + (float)(na * na) <= F.rimg2;
+      const bool okB = i + 1 < nimg &&
+                       (img.inside || (float)(mb * mb) + (float)(nb * nb) <= F.rimg2);
+      // point minus image centre, scaled: u = s w + (c - R)
+      const float2 crx = make_float2(fmaf(-(float)ma, F.a, cx), fmaf(-(float)mb, F.a, cx));
+      const float2 cry = make_float2(fmaf(-(float)na, F.a, cy), fmaf(-(float)nb, F.a, cy));
+      auto U = [&](float2 w, float2 &ux, float2 &uy) {
+        ux = fma2(s2, f2(w.x), crx);
+        uy = fma2(s2, f2(w.y), cry);
+      };
+      auto flush = [&](float2 bp[3], float2 bs[3]) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          if (okA) kahan_add(ph[r], pc[r], bp[r].x);
+          if (okB) kahan_add(ph[r], pc[r], bp[r].y);
+          if (FERM) {
+            if (okA) kahan_add(sp[r], sc[r], bs[r].x);
+            if (okB) kahan_add(sp[r], sc[r], bs[r].y);
+          }
+          bp[r] = bs[r] = f2(0.f);
+        }
+      };
+      float2 bp[3] = {f2(0.f), f2(0.f), f2(0.f)}, bs[3] = {f2(0.f), f2(0.f), f2(0.f)};
+      float2 uAx, uAy, uBx, uBy, uOx, uOy;
+      if (c == 0) {  // the N/2 sub-loop's first segment 1 -> 3
+        float2 u1x, u1y, u3x, u3y;
+        U(w1, u1x, u1y);
+        U(w3, u3x, u3y);
+        const float4 r = lat_seg2_called<FERM>(u1x, u1y, u3x, u3y, il2,
+                                               make_float4(bp[0].x, bp[0].y, bs[0].x, bs[0].y));
+        bp[0] = make_float2(r.x, r.y);
+        bs[0] = make_float2(r.z, r.w);
+      }
+      U(wA, uAx, uAy);
+      U(wB, uBx, uBy);
+      U(wO, uOx, uOy);
+      int q = qa;
+      while (q < qend) {
+        const int qe = min(q + 8, qend);
+#pragma unroll 1
+        for (; q < qe; ++q) {
+          float2 P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
+          U(raw(4 * q), P0x, P0y);
+          U(raw(4 * q + 1), P1x, P1y);
+          U(raw(4 * q + 2), P2x, P2y);
+          U(raw(4 * q + 3), P3x, P3y);
+          lat_seg2<FERM>(uAx, uAy, P0x, P0y, il2, bp[2], bs[2]);  // N/4a: 4q-4 -> 4q
+          lat_seg2<FERM>(uOx, uOy, P1x, P1y, il2, bp[0], bs[0]);  // N/2 : 4q-1 -> 4q+1
+          lat_seg2<FERM>(uBx, uBy, P2x, P2y, il2, bp[1], bs[1]);  // N/4b: 4q-2 -> 4q+2
+          lat_seg2<FERM>(P1x, P1y, P3x, P3y, il2, bp[0], bs[0]);  // N/2 : 4q+1 -> 4q+3
+          uAx = P0x; uAy = P0y;
+          uBx = P2x; uBy = P2y;
+          uOx = P3x; uOy = P3y;
+        }
+        flush(bp, bs);
+      }
+      if (last) {  // closing segments back to points 1, 2, 0
+        float2 ux, uy;
+        float4 r;
+        U(w1, ux, uy);
+        r = lat_seg2_called<FERM>(uOx, uOy, ux, uy, il2,
+                                  make_float4(bp[0].x, bp[0].y, bs[0].x, bs[0].y));
+        bp[0] = make_float2(r.x, r.y);
+        bs[0] = make_float2(r.z, r.w);
+        U(w2, ux, uy);
+        r = lat_seg2_called<FERM>(uBx, uBy, ux, uy, il2,
+                                  make_float4(bp[1].x, bp[1].y, bs[1].x, bs[1].y));
+        bp[1] = make_float2(r.x, r.y);
+        bs[1] = make_float2(r.z, r.w);
+        U(w0, ux, uy);
+        r = lat_seg2_called<FERM>(uAx, uAy, ux, uy, il2,
+                                  make_float4(bp[2].x, bp[2].y, bs[2].x, bs[2].y));
+        bp[2] = make_float2(r.x, r.y);
+        bs[2] = make_float2(r.z, r.w);
+        flush(bp, bs);
+      }
+    }
+    // the chunk's last points carry to the next chunk (image-independent)
+    wA = raw(p1 - 4);
+    wB = raw(p1 - 2);
+    wO = raw(p1 - 1);
+    if (last) {
+      const df G[3] = {fast_two_sum(ph[0], -pc[0]), fast_two_sum(ph[1], -pc[1]),
+                       fast_two_sum(ph[2], -pc[2])};
+      const df H[3] = {fast_two_sum(sp[0], -sc[0]), fast_two_sum(sp[1], -sc[1]),
+                       fast_two_sum(sp[2], -sc[2])};
+      loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
+                          [&](int j, double d0, double d1, double d2) {
+                            S.sacc[3 * j][tid] += d0;
+                            S.sacc[3 * j + 1][tid] += d1;
+                            S.sacc[3 * j + 2][tid] += d2;
+                          });
+    }
+    __syncthreads();
+    if (*S.bad) break;
+    if (tid == 0 && k + kSweepStages < K) issue(k + kSweepStages);
+  }
+  if (*S.bad) {
+    if (tid == 0) {
+      const int kend = min(K, k + kSweepStages);
+      for (int kk = k; kk < kend; ++kk)
+        mbar_wait_bounded(&full_bar[(base + kk) % kSweepStages],
+                          (uint32_t)((base + kk) / kSweepStages) & 1u, A.wait_tries);
+      atomicExch(A.status, kDevTimeout);
+    }
+    consumed = base + K;
+    return false;
+  }
+  consumed = base + K;
+  if (live) {
+    for (int r = 0; r < A.nF * 3; ++r)
+      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + ic] = S.sacc[r][tid];
+  }
+  return true;
+}
+
 // The same tile on packed pairs: thread t runs instances t and t + 128 of a
 // tile of kPairTile, every FP32 operation of the segments as one f32x2
 // operation on the pair (each half rounds as the scalar sweep does); the
@@ -394,7 +639,10 @@ __global__ void __launch_bounds__(kSweepThreads,
   const SweepShared S = {full_bar, sacc, &sm_bad, ring};
   sweep_shared_init(S);
   int consumed = 0;
-  sweep_tile<P, FERM, NINT>(A, blockIdx.x, blockIdx.y, S, consumed);
+  if constexpr (P == kLattice && NINT == 4)
+    sweep_tile_lat<FERM>(A, blockIdx.x, blockIdx.y, S, consumed);
+  else
+    sweep_tile<P, FERM, NINT>(A, blockIdx.x, blockIdx.y, S, consumed);
 }
 
 template <int P, bool FERM, int NINT>

@@ -91,7 +91,8 @@ class ServerStats(C.Structure):
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("p999_ms", C.c_double),
                 ("mean_ms", C.c_double), ("max_ms", C.c_double), ("wall_s", C.c_double),
                 ("segments", C.c_double), ("launches", C.c_longlong),
-                ("resident_ensembles", C.c_int), ("hbm_bytes_in_use", C.c_double)]
+                ("resident_ensembles", C.c_int), ("hbm_bytes_in_use", C.c_double),
+                ("device_busy_s", C.c_double), ("device_span_s", C.c_double)]
 
 
 REQ_W, REQ_LEFF = 0, 1
