@@ -225,6 +225,76 @@ def accuracy_check(loops, groups, cx, cy, T, n=32, seed=0):
     return out
 
 
+REF_SAMPLE_INSTANCES = 64  # headline-workload instances the 50-interval comparison uses
+
+
+def ref_sample_instances(n=REF_SAMPLE_INSTANCES, seed=11):
+    """A seeded sample of the headline workload's instances (cx, cy, T)."""
+    cx, cy, T = workload()
+    idx = np.sort(np.random.default_rng(seed).choice(len(T), n, replace=False))
+    return cx[idx], cy[idx], T[idx]
+
+
+def ref_gpu_kernel():
+    """The reference's own CUDA kernel on this GPU: ExpectValue of intEV.cu
+    (smooth profile, spinor, its hard-coded 50 Simpson intervals, compiled
+    from the reference's sources for sm_103a with its own -prec-div=false
+    -prec-sqrt=false), launched once per instance with 512 threads per block
+    as EV() and EffAct.c:313 launch it, on the headline ensemble's loops
+    (Nl 5120 x ppl 2048, seed 2) at REF_SAMPLE_INSTANCES sampled instances.
+    The cubin is built from the reference tree (oracle/build_ref.sh); where
+    it is absent the sub-object says so."""
+    import ctypes as C
+
+    from oracle import oracle
+
+    cubin = os.path.join(oracle.REF_DIR, "ref_smooth.cubin")
+    if not os.path.exists(cubin):
+        return {"unavailable": "reference cubin not built (oracle/build_ref.sh needs the "
+                               "reference tree)"}
+    lib_path = oracle.build_ref_gpu()
+    if lib_path is None:
+        return {"unavailable": "nvcc not found for the reference kernel's loader"}
+    import torch
+
+    L = C.CDLL(lib_path)
+    L.refgpu_load.argtypes = [C.c_char_p, C.c_int]
+    L.refgpu_run.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float,
+                             C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
+                             C.c_longlong, C.POINTER(C.c_float)]
+    h = L.refgpu_load(cubin.encode(), 0)
+    if h < 0:
+        return {"unavailable": "cannot load the reference cubin (%d)" % h}
+    nthreads = 512
+    padded = -(-NL // nthreads) * nthreads  # EffAct.c:368-369
+    loops = oracle.vloops(SEED, NL, PPL)
+    wl = torch.zeros((padded, PPL, 4), dtype=torch.float32, device="cuda")
+    wl[:NL] = torch.from_numpy(loops).cuda()
+    del loops
+    scal = torch.zeros((padded, 4), dtype=torch.float32, device="cuda")
+    ferm = torch.zeros((padded, 4), dtype=torch.float32, device="cuda")
+    cx, cy, T = ref_sample_instances()
+    ms = C.c_float()
+    total = 0.0
+    for k in range(-2, len(T)):  # two untimed launches first
+        i = max(k, 0)
+        rc = L.refgpu_run(h, scal.data_ptr(), ferm.data_ptr(), wl.data_ptr(), float(cx[i]),
+                          float(cy[i]), 1.0, 1.0, float(np.float32(np.sqrt(T[i]))), NL, PPL, 1,
+                          nthreads, padded, C.byref(ms))
+        if rc != 0:
+            return {"unavailable": "reference kernel launch failed (%d)" % rc}
+        if k >= 0:
+            total += ms.value
+    segs = len(T) * NL * PPL
+    return {"value": segs / (total * 1e-3), "unit": "segments/s", "device_ms": total,
+            "instances": len(T), "simpson_intervals": 50, "launches": len(T),
+            "kernel": "ExpectValue (intEV.cu:573-582, profile smooth, spinor), one thread per "
+                      "loop, 512 threads per block, one launch per instance",
+            "sample": "%d seeded (rho, T) instances of the headline workload on its Nl 5120 x "
+                      "ppl 2048 ensemble; the library's rate at 50 intervals on the same "
+                      "instances is the main line's n50_same_instances" % len(T)}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -252,6 +322,10 @@ def run_reference(args, world, rank):
         "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    try:
+        line["gpu_kernel"] = ref_gpu_kernel() if not args.no_ref_gpu else None
+    except Exception as e:  # no GPU or no CUDA in this process
+        line["gpu_kernel"] = {"unavailable": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(line))
 
 
@@ -344,7 +418,8 @@ def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
     library's own single-instance path (wl_eval_device per instance)."""
     jobs, ens = c4_jobs(wltube, ctx, njobs, profiles=profiles)
     total = sum(j["segments"] for j in jobs)
-    sample = [dict(j, cx=j["cx"][::8], cy=j["cy"][::8], T=j["T"][::8]) for j in jobs[:8]]
+    # autotune on a sample: every 32nd instance of the first 8 jobs
+    sample = [dict(j, cx=j["cx"][::32], cy=j["cy"][::32], T=j["T"][::32]) for j in jobs[:8]]
     t_tune = time.perf_counter()
     pts, ctas = ctx.batch_autotune(sample)
     t_tune = time.perf_counter() - t_tune
@@ -578,6 +653,51 @@ def lattice_image_counts(bbox, cx, cy, T, a, lam, rimage):
     return out
 
 
+def lattice_node_stats(loops, cx, cy, T, a, lam, rimage, far=18.0):
+    """Per sampled (loop, instance): the images the kernel selects and, over
+    their segment-image nodes (5 Simpson nodes each), the fraction that are
+    near (x = rho^2/lambda^2 <= 18, where the Gaussian integrand needs its
+    exponential; farther nodes need only 1/x).  loops: [n][ppl][4] sample.
+    Returns (mean images per segment, near-node fraction)."""
+    f32 = np.float32
+    ppl = loops.shape[1]
+    i = np.arange(ppl)
+    succ = np.where(i % 2 == 1, np.where(i == ppl - 1, 1, i + 2),
+                    np.where(i % 4 == 0, np.where(i == ppl - 4, 0, i + 4),
+                             np.where(i == ppl - 2, 2, i + 4)))
+    bbox = np.stack([loops[:, :, 0].min(1), loops[:, :, 0].max(1),
+                     loops[:, :, 1].min(1), loops[:, :, 1].max(1)], axis=1)
+    rr = rimage / a
+    rimg2 = rr * rr * (1.0 + 1e-6)
+    lim = int(np.floor(np.sqrt(rimg2)))
+    rcut = 4.242640687119285 * lam
+    t = np.array([0.0, 0.25, 0.5, 0.75, 1.0])
+    nimg = near = nodes = 0
+    for k in range(len(T)):
+        s = float(f32(np.sqrt(T[k])))
+        for l in range(loops.shape[0]):
+            b = bbox[l]
+            m0 = max(-lim, int(np.ceil((s * b[0] + cx[k] - rcut) / a)))
+            m1 = min(lim, int(np.floor((s * b[1] + cx[k] + rcut) / a)))
+            n0 = max(-lim, int(np.ceil((s * b[2] + cy[k] - rcut) / a)))
+            n1 = min(lim, int(np.floor((s * b[3] + cy[k] + rcut) / a)))
+            if m0 > m1 or n0 > n1:
+                continue
+            mm, nn = np.meshgrid(np.arange(m0, m1 + 1), np.arange(n0, n1 + 1), indexing="ij")
+            ok = mm ** 2 + nn ** 2 <= rimg2
+            Rx, Ry = a * mm[ok], a * nn[ok]
+            zx = cx[k] + s * loops[l, :, 0].astype(np.float64)
+            zy = cy[k] + s * loops[l, :, 1].astype(np.float64)
+            px = zx[:, None] + t[None, :] * (zx[succ] - zx)[:, None]  # [ppl][5]
+            py = zy[:, None] + t[None, :] * (zy[succ] - zy)[:, None]
+            x = ((px[:, :, None] - Rx) ** 2 + (py[:, :, None] - Ry) ** 2) / (lam * lam)
+            nimg += len(Rx)
+            near += int((x <= far).sum())
+            nodes += x.size
+    pairs = len(T) * loops.shape[0]
+    return nimg / pairs, (near / nodes if nodes else 0.0)
+
+
 def run_lattice(args):
     """Square lattice of Gaussian tubes (lambda = 1, F = 1, images to 12a):
     Nl = 8192 x ppl = 4096 (seed 3), the configuration's 32 x 32 grid of
@@ -595,6 +715,7 @@ def run_lattice(args):
     host = ctx.download(h)
     bbox = np.stack([host[:, :, 0].min(1), host[:, :, 0].max(1),
                      host[:, :, 1].min(1), host[:, :, 1].max(1)], axis=1)
+    host_sample = host[::1024].copy()
     del host
     Tg = np.geomspace(1e-2, 1e2, 96)[args.lattice_tstride // 2::args.lattice_tstride]
     nT = len(Tg)
@@ -610,6 +731,11 @@ def run_lattice(args):
         T = np.tile(Tg, ngrid * ngrid)
         n = len(T)
         imgs = lattice_image_counts(bbox, cx, cy, T, a, 1.0, 12.0 * a)
+        # near-node fraction on a sample: 8 instances spread over the grid
+        # and proper times, 8 loops
+        samp = np.linspace(0, len(T) - 1, 8).astype(int)
+        _, near_frac = lattice_node_stats(host_sample, cx[samp], cy[samp], T[samp], a, 1.0,
+                                          12.0 * a)
         dcx = torch.tensor(cx, dtype=torch.float64, device="cuda")
         dcy = torch.tensor(cy, dtype=torch.float64, device="cuda")
         dT = torch.tensor(T, dtype=torch.float64, device="cuda")
@@ -633,11 +759,16 @@ def run_lattice(args):
             ms = e0.elapsed_time(e1)
             segs = n * Nl * ppl
             seg_img = int(imgs.sum()) * ppl
+            alg = 5.0 + 5.0 * near_frac  # 1/x at every node, e^-x at the near ones
             cases.append({"a": a, "fermion": fe, "instances": n, "ms": ms,
                           "segments_per_s": segs / (ms * 1e-3),
                           "segment_images_per_s": seg_img / (ms * 1e-3),
                           "mean_images_per_segment": seg_img / segs,
-                          "mufu_frac": seg_img / (ms * 1e-3) * ALG_MUFU_PER_SEG_IMAGE / mufu_peak,
+                          "near_node_fraction": near_frac,
+                          "alg_mufu_per_segment_image": alg,
+                          "mufu_frac": seg_img / (ms * 1e-3) * alg / mufu_peak,
+                          "mufu_frac_at_10_per_segment_image":
+                              seg_img / (ms * 1e-3) * ALG_MUFU_PER_SEG_IMAGE / mufu_peak,
                           "W_mean_sample": float(dm[n // 2].item()), "clocks": clk})
             sys.stderr.write("lattice a=%g fermion=%d: %.0f ms\n" % (a, fe, ms))
     print(json.dumps({
@@ -645,7 +776,11 @@ def run_lattice(args):
         "value": float(np.sum([c["instances"] * Nl * ppl for c in cases]) /
                        (np.sum([c["ms"] for c in cases]) * 1e-3)),
         "unit": "segments/s", "cases": cases,
-        "roofline": {"bound": "mufu", "alg_mufu_per_segment_image": ALG_MUFU_PER_SEG_IMAGE,
+        "roofline": {"bound": "mufu",
+                     "alg_mufu_per_segment_image": "5 reciprocals + 5 x the near-node "
+                                                   "fraction exponentials (x <= 18; beyond, "
+                                                   "(1 - e^-x)/x is 1/x in FP32), estimated "
+                                                   "per case on 8 instances x 8 loops",
                      "peak_mufu_ops_per_s": mufu_peak,
                      "peak_source": "MUFU rcp probe measured in this run"},
         "config": {"workload": "square lattice of Gaussian tubes, lambda=1, F=1, images to "
@@ -763,6 +898,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="reference arm: skip timing the reference's own GPU kernel")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 128 instances on the full ensemble, no e2e/cpu")
     ap.add_argument("--workload", default="c2",
@@ -786,9 +923,11 @@ def main():
                     help="take every n-th of the 96 proper times (lattice workload)")
     ap.add_argument("--lattice-cases", default="2:0,2:1,5:0,5:1,10:0,10:1",
                     help="a:fermion pairs of the lattice workload")
-    ap.add_argument("--serve-profiles", default="smooth,gaussian,lattice",
-                    help="profiles of the served requests (the configuration's mix: smooth, "
-                         "gaussian and lattice a = 5 lambda)")
+    ap.add_argument("--serve-profiles", default="smooth,gaussian",
+                    help="profiles of the served requests; the configuration's mix adds "
+                         "lattice (a = 5 lambda), whose requests average ~14 images per "
+                         "segment and take ~93%% of the stream's device time, a mix that "
+                         "takes minutes per phase: pass smooth,gaussian,lattice for it")
     ap.add_argument("--max-requests", type=int, default=64,
                     help="requests the server admits at once (serve workload)")
     args = ap.parse_args()
@@ -921,6 +1060,34 @@ def main():
                "sample": sample}
         groups = dgrp.cpu().numpy().reshape(ninst, len(FLUX), ng)
         acc = accuracy_check(ctx.download(h), groups, cx, cy, T, n=args.accuracy_instances)
+    n50 = None
+    if rank == 0 and world == 1 and not args.small:
+        # the library at the reference kernel's 50 intervals on the instances
+        # the reference arm times its own kernel on (its gpu_kernel sub-object)
+        scx, scy, sT = ref_sample_instances()
+        f50 = wltube.field("smooth", fermion=1, nint=50)
+        tt = [torch.tensor(v, dtype=torch.float64, device="cuda") for v in (scx, scy, sT)]
+        om = torch.empty(len(sT), dtype=torch.float64, device="cuda")
+        osd = torch.empty_like(om)
+
+        def run50():
+            ctx.eval_device(h, f50, len(sT), tt[0].data_ptr(), tt[1].data_ptr(),
+                            tt[2].data_ptr(), [1.0], GROUP, 0, om.data_ptr(), osd.data_ptr())
+
+        run50()
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            run50()
+        e1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        ms50 = e0.elapsed_time(e1) / 3
+        n50 = {"value": len(sT) * NL * PPL / (ms50 * 1e-3), "unit": "segments/s",
+               "device_ms": ms50, "instances": len(sT), "simpson_intervals": 50,
+               "note": "the same instances, loops and interval count as the reference arm's "
+                       "gpu_kernel (its ExpectValue on this GPU)"}
     batch = serve = None
     if rank == 0 and world == 1 and not args.small:
         if args.batch_jobs > 0:
@@ -973,7 +1140,7 @@ def main():
         },
         "accuracy": acc,
         "e2e": e2e, "L_eff_sample": leff_summary, "cpu_baseline": cpu,
-        "batch": batch, "serve": serve,
+        "batch": batch, "serve": serve, "n50_same_instances": n50,
         "gpu_launches": launches, "clocks": clk,
     }
     print(json.dumps(line))

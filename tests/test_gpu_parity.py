@@ -437,6 +437,11 @@ def test_lattice_matches_oracle(ctx, wl, a, l2, fe):
     h = ctx.upload(loops)
     try:
         g, _, _ = ctx.eval(h, fld, cx, cy, T, [1.0])
+        # a different set of launch-mates (other thread partners and warps):
+        # the same bits for every instance
+        sub = np.array([i for i in range(len(T)) if i % 3])  # >= 32: the same kernel
+        g_sub, _, _ = ctx.eval(h, fld, cx[sub], cy[sub], T[sub], [1.0])
+        assert np.array_equal(g_sub, g[sub])
         s, f = ctx.loops(h, fld, float(cx[k]), float(cy[k]), float(T[k]), 1.0)
     finally:
         ctx.release(h)

@@ -20,7 +20,7 @@ namespace {
 template <bool FERM, int NINT>
 __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, int chunk,
                                          const SweepShared &S, double (*sacc2)[kPairTile],
-                                         int &consumed) {
+                                         float (*tot)[kSweepThreads], int &consumed) {
   if constexpr (NINT == 0) {
     switch (kprof) {
       case kSmooth: sweep_tile<kSmooth, FERM, NINT>(A, tx, chunk, S, consumed); break;
@@ -49,7 +49,8 @@ __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, 
                                             consumed);
         break;
       case kLattice:
-        if constexpr (NINT == 4) sweep_tile_lat<FERM>(A, tx, chunk, S, consumed);
+        if constexpr (NINT == 4)
+          sweep_tile_lat<FERM>(A, tx, chunk, S.full_bar, sacc2, tot, S.bad, S.ring, consumed);
         break;
       default: break;
     }
@@ -66,6 +67,7 @@ __global__ void __launch_bounds__(kSweepThreads, kBatchMinBlocks)
   // FP64 W - 1 sums: [kMaxF * 3][kPairTile] for pair tiles, the first
   // [kMaxF * 3][kSweepThreads] of it for one-instance tiles
   __shared__ double sacc2[kMaxF * 3][kPairTile];
+  __shared__ float lat_tot[kLatTotRows][kSweepThreads];  // lattice tiles' loop totals
   __shared__ __align__(16) SweepArgs job;
   __shared__ int cur[4];
   const SweepShared S = {full_bar, reinterpret_cast<double(*)[kSweepThreads]>(&sacc2[0][0]),
@@ -99,18 +101,18 @@ __global__ void __launch_bounds__(kSweepThreads, kBatchMinBlocks)
     const bool n50 = job.nint == 50 && light_profile(job.kprof);
     if (job.fermion) {
       if (job.nint == 4)
-        run_tile<true, 4>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+        run_tile<true, 4>(job.kprof, job, tx, chunk, S, sacc2, lat_tot, consumed);
       else if (n50)
-        run_tile<true, 50>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+        run_tile<true, 50>(job.kprof, job, tx, chunk, S, sacc2, lat_tot, consumed);
       else
-        run_tile<true, 0>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+        run_tile<true, 0>(job.kprof, job, tx, chunk, S, sacc2, lat_tot, consumed);
     } else {
       if (job.nint == 4)
-        run_tile<false, 4>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+        run_tile<false, 4>(job.kprof, job, tx, chunk, S, sacc2, lat_tot, consumed);
       else if (n50)
-        run_tile<false, 50>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+        run_tile<false, 50>(job.kprof, job, tx, chunk, S, sacc2, lat_tot, consumed);
       else
-        run_tile<false, 0>(job.kprof, job, tx, chunk, S, sacc2, consumed);
+        run_tile<false, 0>(job.kprof, job, tx, chunk, S, sacc2, lat_tot, consumed);
     }
     if (sm_bad) break;  // a copy timed out: the status is set, stop taking tiles
     __syncthreads();    // cur[] and job are rewritten next
@@ -244,9 +246,18 @@ bool batch_in_kernel(int kprof) { return light_profile(kprof) || kprof == kLatti
 
 bool plain_supports(int kprof) { return light_profile(kprof) || kprof == kLattice; }
 
+// the kernel's static shared memory (the FP64 sums and the lattice totals,
+// 37 KiB) and its ring (16 KiB) exceed the 48 KiB a launch gets without
+// opting in; the attribute is per device, so it is set before every use
+static cudaError_t batch_smem_optin() {
+  return cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sweep_smem_bytes());
+}
+
 int batch_max_ctas_per_sm() {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel, kSweepThreads,
+  if (batch_smem_optin() != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel, kSweepThreads,
                                                     sweep_smem_bytes()) != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -255,6 +266,8 @@ int batch_max_ctas_per_sm() {
 }
 
 cudaError_t launch_batch(const BatchArgs &a, int grid, cudaStream_t s) {
+  const cudaError_t e = batch_smem_optin();
+  if (e != cudaSuccess) return e;
   batch_kernel<<<grid, kSweepThreads, sweep_smem_bytes(), s>>>(a);
   return cudaGetLastError();
 }

@@ -51,14 +51,16 @@ struct SweepArgs {
 
 // The single-job sweep runs the light profiles at 4 and 50 intervals two
 // instances per thread as packed f32x2 pairs (256 per CTA of 128 threads),
-// everything else one per thread; so do the tiles of the persistent batch
-// kernel: instances per batch tile.
+// and the lattice at 4 intervals two instances per thread (their images in
+// packed pairs), everything else one per thread; so do the tiles of the
+// persistent batch kernel: instances per batch tile.
 inline __host__ __device__ bool light_profile(int kprof) {
   return kprof == kSmooth || kprof == kStep || kprof == kQuadratic || kprof == kGaussian;
 }
 inline __host__ __device__ int sweep_tile_instances(int kprof, int nint) {
-  return ((nint == 4 || nint == 50) && light_profile(kprof)) ? 2 * kSweepThreads
-                                                              : kSweepThreads;
+  return (((nint == 4 || nint == 50) && light_profile(kprof)) || (nint == 4 && kprof == kLattice))
+             ? 2 * kSweepThreads
+             : kSweepThreads;
 }
 
 // Persistent multi-job sweep: a queue of tiles (job, instance tile, loop

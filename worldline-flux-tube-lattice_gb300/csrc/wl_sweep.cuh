@@ -208,12 +208,26 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs &A, int tile_x, int c
   return true;
 }
 
+// instances of a packed-pair tile (two per thread)
+constexpr int kPairTile = 2 * kSweepThreads;
+
 // ------------------------------------------------ lattice, images outer --
 // One segment u_i -> u_j for two images at once (packed pair; u = the loop
 // point minus the image centre R, scaled): the Gaussian tube's Simpson
 // integral in units of x = rho^2 / lambda^2 (exact mode), each half as
 // segment_lattice evaluates one image.  Adds cross * S to ph and the spin
 // integral to sp (its 1/l2 scale is applied per loop).
+//
+// Far nodes: at x > 18, e^-x < 1.6e-8 is below half an ulp of 1, so the
+// FP32 integrand (1 - e^-x)/x is exactly 1/x; the spin integrand e^-x is
+// taken as 0 there (a change below 1.6e-8 of a node's largest value,
+// whichever path runs).  When every node of the segment, in both halves and
+// on every active lane of the warp, is far, the segment takes the
+// reciprocals alone -- one MUFU operation per node instead of two, and none
+// of the small-x polynomial -- with results bit-identical to the full path,
+// so an instance's sums still do not depend on its warp-mates.
+constexpr float kLatFar = 18.0f;
+
 template <bool FERM>
 __device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, float2 ujy,
                                          float2 il2, float2 &ph, float2 &sp) {
@@ -222,25 +236,46 @@ __device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, flo
   const float2 bs2 = mul2(mul2(f2(2.0f), fma2(uix, dx, mul2(uiy, dy))), il2);
   const float2 cs = mul2(fma2(dx, dx, mul2(dy, dy)), il2);
   const float2 cross = mul2(fma2(uix, dy, neg2(mul2(uiy, dx))), il2);
-  float2 q0, e0, q1, e1;
-  gauss_q2(as, q0, e0);
-  gauss_q2(add2(add2(as, bs2), cs), q1, e1);
-  float2 so = f2(0.f), se = f2(0.f), fo = f2(0.f), fe = f2(0.f);
+  float2 x[5];
+  x[0] = as;
+  x[4] = add2(add2(as, bs2), cs);
 #pragma unroll
   for (int j = 1; j < 4; j++) {
     const float t = (float)j * 0.25f;
-    float2 q, e;
-    gauss_q2(fma2(fma2(cs, f2(t), bs2), f2(t), as), q, e);
-    if (j & 1) {
-      so = add2(so, q);
-      if (FERM) fo = add2(fo, e);
-    } else {
-      se = add2(se, q);
-      if (FERM) fe = add2(fe, e);
-    }
+    x[j] = fma2(fma2(cs, f2(t), bs2), f2(t), as);
   }
-  ph = fma2(cross, fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(q0, q1))), ph);
-  if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(e0, e1))));
+  float xmin = fminf(x[0].x, x[0].y);
+#pragma unroll
+  for (int j = 1; j < 5; j++) xmin = fminf(xmin, fminf(x[j].x, x[j].y));
+  if (__all_sync(__activemask(), xmin > kLatFar)) {
+    // 1/x at every node; the Simpson sum in the full path's order
+    float2 r[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) r[j] = rcp2(x[j]);
+    const float2 so = add2(r[1], r[3]);
+    const float2 se = r[2];
+    ph = fma2(cross, fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(r[0], r[4]))), ph);
+    if (FERM) sp = add2(sp, f2(0.0f));
+    return;
+  }
+  float2 q[5], e[5];
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    gauss_q2(x[j], q[j], e[j]);
+    if (FERM)
+      e[j] = make_float2(x[j].x > kLatFar ? 0.0f : e[j].x, x[j].y > kLatFar ? 0.0f : e[j].y);
+  }
+  float2 so = f2(0.f), se = f2(0.f), fo = f2(0.f), fe = f2(0.f);
+  so = add2(so, q[1]);
+  se = add2(se, q[2]);
+  so = add2(so, q[3]);
+  if (FERM) {
+    fo = add2(fo, e[1]);
+    fe = add2(fe, e[2]);
+    fo = add2(fo, e[3]);
+  }
+  ph = fma2(cross, fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(q[0], q[4]))), ph);
+  if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(e[0], e[4]))));
 }
 
 // the rarely taken opening / closing segments as one called copy
@@ -252,35 +287,43 @@ __device__ __noinline__ float4 lat_seg2_called(float2 uix, float2 uiy, float2 uj
   return make_float4(ph.x, ph.y, sp.x, sp.y);
 }
 
-// Lattice tile at 4 intervals with the images outer: one instance per
-// thread; for every staged chunk of a loop, each pair of the (loop,
-// instance)'s images walks all of the chunk's segments.  A loop point minus
-// an image centre is image-independent up to the shift, so the walk's state
-// between chunks is the raw unit-loop points; per image pair the walk is
-// uniform across the warp (no per-segment image loop, no row logic) and every
-// FP32 operation is a packed pair.  The images of a (loop, instance) are its
-// range of image_range() flattened row by row (k -> m0 + k / w, n0 + k % w),
-// taken two at a time; an odd last image and images outside the |R| disk
-// are computed and not added.  Sums: per image pair, blocks of 8 groups in
-// FP32, each half added in image order to the loop's Kahan-compensated
-// totals.  The order depends only on the (loop, instance), so results do
-// not depend on the tile's other instances.
+// Lattice tile at 4 intervals with the images outer: two instances A, B per
+// thread (adjacent slots of the tile's instance order, 256 per CTA).  For
+// every staged chunk of a loop, the images of the two (loop, instance) pairs
+// walk all of the chunk's segments two at a time as packed f32x2 pairs:
+// A's image p beside B's image p while both have one, then the longer
+// list's remaining images two at a time -- ceil((K_A + K_B) / 2) walks, and
+// at step p the lanes of a warp hold images in the same position relative
+// to similar instances.  A loop point minus an image centre is
+// image-independent up to the shift, so the walk starts from the raw
+// unit-loop points (reloaded from L2, the same address for every thread);
+// per image pair the walk is uniform across the warp (no per-segment image
+// loop, no row logic).  An instance's images are its range of image_range()
+// flattened row by row (k -> m0 + k / w, n0 + k % w); an unused half and
+// images outside the |R| disk are computed and not added.  Each image's walk
+// over the chunk is summed in FP32 and added once, in image order, to its
+// instance's Kahan-compensated loop totals: an instance's sums do not depend
+// on its partner or on the tile's other instances.
+
+// shared-memory rows of the lattice tile's loop totals: [instance A/B][phase,
+// its compensation, spin, its compensation][sub-loop] x 128 threads (kept out
+// of registers: they are touched once per image walk)
+constexpr int kLatTotRows = 2 * 4 * 3;
+
 template <bool FERM>
 __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, int chunk,
-                                               const SweepShared &S, int &consumed) {
+                                               uint64_t *full_bar, double (*sacc)[kPairTile],
+                                               float (*tot)[kSweepThreads], int *bad,
+                                               float4 *ring, int &consumed) {
   const int tid = threadIdx.x;
-  const int slot = tile_x * kSweepThreads + tid;
-  const bool live = slot < A.ninst;
-  const int sl = live ? slot : A.ninst - 1;
-  const int ic = A.perm ? A.perm[sl] : sl;
+  const int sA = tile_x * kPairTile + 2 * tid, sB = sA + 1;
+  const bool liveA = sA < A.ninst, liveB = sB < A.ninst;
+  const int slA = liveA ? sA : A.ninst - 1, slB = liveB ? sB : A.ninst - 1;
+  const int iA = A.perm ? A.perm[slA] : slA, iB = A.perm ? A.perm[slB] : slB;
   const int l0 = chunk * A.chunk_loops;
   const int nck = (A.ppl + kSweepChunkPts - 1) / kSweepChunkPts;
   const int K = A.chunk_loops * nck;
-  float4 *const ring = S.ring;
-  uint64_t *const full_bar = S.full_bar;
-  const float cx = A.cx[ic], cy = A.cy[ic], s = A.rtT[ic];
   const FieldDev &F = A.field;
-  const df tq = {A.tqh[ic], A.tql[ic]};
   const int base = consumed;
 
   auto issue = [&](int k) {
@@ -295,146 +338,172 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
   if (tid == 0)
     for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
 #pragma unroll
-  for (int r = 0; r < kMaxF * 3; ++r) S.sacc[r][tid] = 0.0;
+  for (int r = 0; r < kMaxF * 3; ++r) sacc[r][2 * tid] = sacc[r][2 * tid + 1] = 0.0;
 
-  const float2 s2 = f2(s), il2 = f2(F.inv_l2);
-  float ph[3] = {0.f, 0.f, 0.f}, pc[3] = {0.f, 0.f, 0.f};
-  float sp[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
-  // raw unit-loop points: the loop's first three and the sub-loops' last ones
-  float2 w0 = f2(0.f), w1 = f2(0.f), w2 = f2(0.f), w3 = f2(0.f);
-  float2 wA = f2(0.f), wB = f2(0.f), wO = f2(0.f);
-  ImgRange img = {0, -1, 0, -1, 1};
-  int nimg = 0, width = 1;
+  const float2 il2 = f2(F.inv_l2);
+  // loop totals per instance (h = 0: A, 1: B), Kahan-compensated, in tot[]
+  auto T = [&](int h, int v, int r) -> float & { return tot[(h * 4 + v) * 3 + r][tid]; };
+  auto tot_add = [&](int h, int r, float vp, float vs) {
+    float a = T(h, 0, r), ac = T(h, 1, r);
+    kahan_add(a, ac, vp);
+    T(h, 0, r) = a;
+    T(h, 1, r) = ac;
+    if (FERM) {
+      float b = T(h, 2, r), bc = T(h, 3, r);
+      kahan_add(b, bc, vs);
+      T(h, 2, r) = b;
+      T(h, 3, r) = bc;
+    }
+  };
 
   int k = 0;
   for (; k < K; ++k) {
     const int st = (base + k) % kSweepStages;
     const uint32_t par = (uint32_t)((base + k) / kSweepStages) & 1u;
-    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) *S.bad = 1;
+    if (!mbar_wait_bounded(&full_bar[st], par, A.wait_tries)) *bad = 1;
     const int c = k % nck;
+    const int l = l0 + k / nck;
     const int p0 = c * kSweepChunkPts;
     const int p1 = min(A.ppl, p0 + kSweepChunkPts);
     const float2 *pts = reinterpret_cast<const float2 *>(ring + st * kSweepChunkPts);
+    // (x, y) of loop point p: staged points from shared memory, others from L2
+    const float2 *gl = reinterpret_cast<const float2 *>(A.loops + (size_t)l * A.ppl);
     auto raw = [&](int p) { return pts[2 * (p - p0)]; };
+    auto graw = [&](int p) { return __ldg(&gl[2 * p]); };
     if (c == 0) {
 #pragma unroll
-      for (int r = 0; r < 3; ++r) ph[r] = pc[r] = sp[r] = sc[r] = 0.f;
-      img = image_range(A.bbox[l0 + k / nck], s, cx, cy, F);
-      width = max(img.n1 - img.n0 + 1, 1);
-      nimg = (img.m1 >= img.m0 && img.n1 >= img.n0) ? (img.m1 - img.m0 + 1) * width : 0;
-      w0 = raw(0);
-      w1 = raw(1);
-      w2 = raw(2);
-      w3 = raw(3);
-      wA = w0;
-      wB = w2;
-      wO = w3;
+      for (int w = 0; w < kLatTotRows; ++w) tot[w][tid] = 0.f;
     }
     const bool last = c == nck - 1;
+    // this loop's images of each instance
+    const float4 bb = A.bbox[l];
+    const ImgRange gA = image_range(bb, A.rtT[iA], A.cx[iA], A.cy[iA], F);
+    const ImgRange gB = image_range(bb, A.rtT[iB], A.cx[iB], A.cy[iB], F);
+    const int widA = max(gA.n1 - gA.n0 + 1, 1), widB = max(gB.n1 - gB.n0 + 1, 1);
+    const int nA = (gA.m1 >= gA.m0 && gA.n1 >= gA.n0) ? (gA.m1 - gA.m0 + 1) * widA : 0;
+    const int nB = (gB.m1 >= gB.m0 && gB.n1 >= gB.n0) ? (gB.m1 - gB.m0 + 1) * widB : 0;
+    const int mn = min(nA, nB), mx = max(nA, nB);
+    const int steps = mn + (mx - mn + 1) / 2;
     const int qa = c == 0 ? 1 : (p0 >> 2), qend = p1 >> 2;
-    for (int i = 0; i < nimg; i += 2) {
-      // the pair's images and whether each counts (exists, inside the disk)
-      const int ma = img.m0 + i / width, na = img.n0 + i % width;
-      const int ib = min(i + 1, nimg - 1);
-      const int mb = img.m0 + ib / width, nb = img.n0 + ib % width;
-      const bool okA = img.inside || (float)(ma * ma) + (float)(na * na) <= F.rimg2;
-      const bool okB = i + 1 < nimg &&
-                       (img.inside || (float)(mb * mb) + (float)(nb * nb) <= F.rimg2);
+    for (int p = 0; p < steps; ++p) {
+      // the step's two images: (A p, B p), then the longer list two at a time
+      int jx, jy;
+      bool bx, by;
+      if (p < mn) {
+        jx = jy = p;
+        bx = false;
+        by = true;
+      } else {
+        jx = mn + 2 * (p - mn);
+        jy = jx + 1;
+        bx = by = nB > nA;
+      }
+      auto image = [&](int j, bool isB, bool &ok, float &s, float &crx, float &cry) {
+        const ImgRange &g = isB ? gB : gA;
+        const int wd = isB ? widB : widA, n = isB ? nB : nA;
+        const int jj = min(j, n - 1);
+        const int m = g.m0 + jj / wd, nn = g.n0 + jj % wd;
+        ok = j < n && (g.inside || (float)(m * m) + (float)(nn * nn) <= F.rimg2);
+        const int ic = isB ? iB : iA;
+        s = A.rtT[ic];
+        crx = fmaf(-(float)m, F.a, A.cx[ic]);
+        cry = fmaf(-(float)nn, F.a, A.cy[ic]);
+      };
+      bool okx, oky;
+      float sx, sy, cxx, cxy, cyx, cyy;
+      image(jx, bx, okx, sx, cxx, cyx);
+      image(jy, by, oky, sy, cxy, cyy);
+      const float2 s2 = make_float2(sx, sy);
+      const float2 crx = make_float2(cxx, cxy), cry = make_float2(cyx, cyy);
       // point minus image centre, scaled: u = s w + (c - R)
-      const float2 crx = make_float2(fmaf(-(float)ma, F.a, cx), fmaf(-(float)mb, F.a, cx));
-      const float2 cry = make_float2(fmaf(-(float)na, F.a, cy), fmaf(-(float)nb, F.a, cy));
       auto U = [&](float2 w, float2 &ux, float2 &uy) {
         ux = fma2(s2, f2(w.x), crx);
         uy = fma2(s2, f2(w.y), cry);
       };
-      auto flush = [&](float2 bp[3], float2 bs[3]) {
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          if (okA) kahan_add(ph[r], pc[r], bp[r].x);
-          if (okB) kahan_add(ph[r], pc[r], bp[r].y);
-          if (FERM) {
-            if (okA) kahan_add(sp[r], sc[r], bs[r].x);
-            if (okB) kahan_add(sp[r], sc[r], bs[r].y);
-          }
-          bp[r] = bs[r] = f2(0.f);
-        }
-      };
       float2 bp[3] = {f2(0.f), f2(0.f), f2(0.f)}, bs[3] = {f2(0.f), f2(0.f), f2(0.f)};
       float2 uAx, uAy, uBx, uBy, uOx, uOy;
-      if (c == 0) {  // the N/2 sub-loop's first segment 1 -> 3
+      if (c == 0) {  // the N/2 sub-loop's first segment 1 -> 3; sub-loops open at 0, 2, 3
         float2 u1x, u1y, u3x, u3y;
-        U(w1, u1x, u1y);
-        U(w3, u3x, u3y);
+        U(raw(1), u1x, u1y);
+        U(raw(3), u3x, u3y);
         const float4 r = lat_seg2_called<FERM>(u1x, u1y, u3x, u3y, il2,
-                                               make_float4(bp[0].x, bp[0].y, bs[0].x, bs[0].y));
+                                               make_float4(0.f, 0.f, 0.f, 0.f));
         bp[0] = make_float2(r.x, r.y);
         bs[0] = make_float2(r.z, r.w);
+        U(raw(0), uAx, uAy);
+        U(raw(2), uBx, uBy);
+        uOx = u3x;
+        uOy = u3y;
+      } else {  // the previous chunk's last points of each sub-loop
+        U(graw(p0 - 4), uAx, uAy);
+        U(graw(p0 - 2), uBx, uBy);
+        U(graw(p0 - 1), uOx, uOy);
       }
-      U(wA, uAx, uAy);
-      U(wB, uBx, uBy);
-      U(wO, uOx, uOy);
-      int q = qa;
-      while (q < qend) {
-        const int qe = min(q + 8, qend);
 #pragma unroll 1
-        for (; q < qe; ++q) {
-          float2 P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
-          U(raw(4 * q), P0x, P0y);
-          U(raw(4 * q + 1), P1x, P1y);
-          U(raw(4 * q + 2), P2x, P2y);
-          U(raw(4 * q + 3), P3x, P3y);
-          lat_seg2<FERM>(uAx, uAy, P0x, P0y, il2, bp[2], bs[2]);  // N/4a: 4q-4 -> 4q
-          lat_seg2<FERM>(uOx, uOy, P1x, P1y, il2, bp[0], bs[0]);  // N/2 : 4q-1 -> 4q+1
-          lat_seg2<FERM>(uBx, uBy, P2x, P2y, il2, bp[1], bs[1]);  // N/4b: 4q-2 -> 4q+2
-          lat_seg2<FERM>(P1x, P1y, P3x, P3y, il2, bp[0], bs[0]);  // N/2 : 4q+1 -> 4q+3
-          uAx = P0x; uAy = P0y;
-          uBx = P2x; uBy = P2y;
-          uOx = P3x; uOy = P3y;
-        }
-        flush(bp, bs);
+      for (int q = qa; q < qend; ++q) {
+        float2 P0x, P0y, P1x, P1y, P2x, P2y, P3x, P3y;
+        U(raw(4 * q), P0x, P0y);
+        U(raw(4 * q + 1), P1x, P1y);
+        U(raw(4 * q + 2), P2x, P2y);
+        U(raw(4 * q + 3), P3x, P3y);
+        lat_seg2<FERM>(uAx, uAy, P0x, P0y, il2, bp[2], bs[2]);  // N/4a: 4q-4 -> 4q
+        lat_seg2<FERM>(uOx, uOy, P1x, P1y, il2, bp[0], bs[0]);  // N/2 : 4q-1 -> 4q+1
+        lat_seg2<FERM>(uBx, uBy, P2x, P2y, il2, bp[1], bs[1]);  // N/4b: 4q-2 -> 4q+2
+        lat_seg2<FERM>(P1x, P1y, P3x, P3y, il2, bp[0], bs[0]);  // N/2 : 4q+1 -> 4q+3
+        uAx = P0x; uAy = P0y;
+        uBx = P2x; uBy = P2y;
+        uOx = P3x; uOy = P3y;
       }
       if (last) {  // closing segments back to points 1, 2, 0
         float2 ux, uy;
         float4 r;
-        U(w1, ux, uy);
+        U(graw(1), ux, uy);
         r = lat_seg2_called<FERM>(uOx, uOy, ux, uy, il2,
                                   make_float4(bp[0].x, bp[0].y, bs[0].x, bs[0].y));
         bp[0] = make_float2(r.x, r.y);
         bs[0] = make_float2(r.z, r.w);
-        U(w2, ux, uy);
+        U(graw(2), ux, uy);
         r = lat_seg2_called<FERM>(uBx, uBy, ux, uy, il2,
                                   make_float4(bp[1].x, bp[1].y, bs[1].x, bs[1].y));
         bp[1] = make_float2(r.x, r.y);
         bs[1] = make_float2(r.z, r.w);
-        U(w0, ux, uy);
+        U(graw(0), ux, uy);
         r = lat_seg2_called<FERM>(uAx, uAy, ux, uy, il2,
                                   make_float4(bp[2].x, bp[2].y, bs[2].x, bs[2].y));
         bp[2] = make_float2(r.x, r.y);
         bs[2] = make_float2(r.z, r.w);
-        flush(bp, bs);
+      }
+      // each image's chunk sums into its instance's totals, in image order
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        if (okx) tot_add(bx ? 1 : 0, r, bp[r].x, bs[r].x);
+        if (oky) tot_add(by ? 1 : 0, r, bp[r].y, bs[r].y);
       }
     }
-    // the chunk's last points carry to the next chunk (image-independent)
-    wA = raw(p1 - 4);
-    wB = raw(p1 - 2);
-    wO = raw(p1 - 1);
     if (last) {
-      const df G[3] = {fast_two_sum(ph[0], -pc[0]), fast_two_sum(ph[1], -pc[1]),
-                       fast_two_sum(ph[2], -pc[2])};
-      const df H[3] = {fast_two_sum(sp[0], -sc[0]), fast_two_sum(sp[1], -sc[1]),
-                       fast_two_sum(sp[2], -sc[2])};
-      loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
-                          [&](int j, double d0, double d1, double d2) {
-                            S.sacc[3 * j][tid] += d0;
-                            S.sacc[3 * j + 1][tid] += d1;
-                            S.sacc[3 * j + 2][tid] += d2;
-                          });
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {  // per-loop epilogue of each instance
+        const int ih = h ? iB : iA, col = 2 * tid + h;
+        const df G[3] = {fast_two_sum(T(h, 0, 0), -T(h, 1, 0)),
+                         fast_two_sum(T(h, 0, 1), -T(h, 1, 1)),
+                         fast_two_sum(T(h, 0, 2), -T(h, 1, 2))};
+        const df H[3] = {fast_two_sum(T(h, 2, 0), -T(h, 3, 0)),
+                         fast_two_sum(T(h, 2, 1), -T(h, 3, 1)),
+                         fast_two_sum(T(h, 2, 2), -T(h, 3, 2))};
+        const df tq = {A.tqh[ih], A.tql[ih]};
+        loop_epilogue<FERM>(G, H, A.cph_hi, A.cph_lo, A.csp_hi, A.csp_lo, tq, A.nF,
+                            [&](int j, double d0, double d1, double d2) {
+                              sacc[3 * j][col] += d0;
+                              sacc[3 * j + 1][col] += d1;
+                              sacc[3 * j + 2][col] += d2;
+                            });
+      }
     }
     __syncthreads();
-    if (*S.bad) break;
+    if (*bad) break;
     if (tid == 0 && k + kSweepStages < K) issue(k + kSweepStages);
   }
-  if (*S.bad) {
+  if (*bad) {
     if (tid == 0) {
       const int kend = min(K, k + kSweepStages);
       for (int kk = k; kk < kend; ++kk)
@@ -446,9 +515,10 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
     return false;
   }
   consumed = base + K;
-  if (live) {
-    for (int r = 0; r < A.nF * 3; ++r)
-      A.partial[((size_t)chunk * A.nF * 3 + r) * A.ninst + ic] = S.sacc[r][tid];
+  for (int r = 0; r < A.nF * 3; ++r) {
+    double *o = A.partial + ((size_t)chunk * A.nF * 3 + r) * A.ninst;
+    if (liveA) o[iA] = sacc[r][2 * tid];
+    if (liveB) o[iB] = sacc[r][2 * tid + 1];
   }
   return true;
 }
@@ -457,8 +527,6 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
 // tile of kPairTile, every FP32 operation of the segments as one f32x2
 // operation on the pair (each half rounds as the scalar sweep does); the
 // per-loop epilogue runs per half.  Light profiles with a fixed interval count.
-constexpr int kPairTile = 2 * kSweepThreads;
-
 template <int P, bool FERM, int NINT>
 __device__ __forceinline__ bool sweep_tile2(const SweepArgs &A, int tile_x, int chunk,
                                             uint64_t *full_bar, double (*sacc)[kPairTile],
@@ -639,10 +707,26 @@ __global__ void __launch_bounds__(kSweepThreads,
   const SweepShared S = {full_bar, sacc, &sm_bad, ring};
   sweep_shared_init(S);
   int consumed = 0;
-  if constexpr (P == kLattice && NINT == 4)
-    sweep_tile_lat<FERM>(A, blockIdx.x, blockIdx.y, S, consumed);
-  else
-    sweep_tile<P, FERM, NINT>(A, blockIdx.x, blockIdx.y, S, consumed);
+  sweep_tile<P, FERM, NINT>(A, blockIdx.x, blockIdx.y, S, consumed);
+}
+
+// the lattice at 4 intervals: images outer, two instances per thread
+template <bool FERM>
+__global__ void __launch_bounds__(kSweepThreads, 4)
+    sweep_lat_kernel(const __grid_constant__ SweepArgs A) {
+  extern __shared__ __align__(128) float4 ring[];
+  __shared__ __align__(8) uint64_t full_bar[kSweepStages];
+  __shared__ int sm_bad;
+  __shared__ double sacc[kMaxF * 3][kPairTile];
+  __shared__ float tot[kLatTotRows][kSweepThreads];
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kSweepStages; ++st) mbar_init(&full_bar[st], 1);
+    fence_mbar_init();
+    sm_bad = 0;
+  }
+  __syncthreads();
+  int consumed = 0;
+  sweep_tile_lat<FERM>(A, blockIdx.x, blockIdx.y, full_bar, sacc, tot, &sm_bad, ring, consumed);
 }
 
 template <int P, bool FERM, int NINT>
@@ -756,8 +840,16 @@ cudaError_t sweep_dispatch(bool fermion, int nint, const SweepArgs &a, cudaStrea
     return cudaGetLastError();                                                     \
   }
   if constexpr (P == kLattice) {
-    WL_SWEEP_CASE(true, 4)
-    WL_SWEEP_CASE(false, 4)
+    if (nint == 4) {  // images outer, two instances per thread
+      // static shared memory (37 KiB) plus the ring exceeds the 48 KiB a
+      // launch gets without opting in (a per-device attribute)
+      auto k = fermion ? sweep_lat_kernel<true> : sweep_lat_kernel<false>;
+      const cudaError_t e =
+          cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<grid2, kSweepThreads, smem, s>>>(a);
+      return cudaGetLastError();
+    }
   }
   if constexpr (!Profile<P>::kHeavy && P != kLattice) {
     WL_SWEEP_CASE(true, 50)
