@@ -420,9 +420,16 @@ def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
     total = sum(j["segments"] for j in jobs)
     # autotune on a sample: every 32nd instance of the first 8 jobs
     sample = [dict(j, cx=j["cx"][::32], cy=j["cy"][::32], T=j["T"][::32]) for j in jobs[:8]]
+    # the sample at the default shape (16384 points per tile, occupancy-limit
+    # CTAs per SM), then tuned: what the autotuner buys on this mix
+    ctx.batch_eval(sample, graph=True)
+    ctx.batch_eval(sample, graph=True)
+    ms_default = ctx.batch_stats()["device_ms"]
     t_tune = time.perf_counter()
     pts, ctas = ctx.batch_autotune(sample)
     t_tune = time.perf_counter() - t_tune
+    ctx.batch_eval(sample, graph=True)
+    ms_tuned = ctx.batch_stats()["device_ms"]
     for _ in range(warmup):
         ctx.batch_eval(jobs, graph=True)
     ms = []
@@ -450,7 +457,11 @@ def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
         "value": batched, "unit": "segments/s", "ms_per_step": bms, "steps": steps,
         "warmup": warmup, "jobs": len(jobs), "segments_per_step": int(total),
         "tiles": st["tiles"], "grid": st["grid"],
-        "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas, "seconds": t_tune},
+        "autotune": {"points_per_tile": pts, "ctas_per_sm": ctas, "seconds": t_tune,
+                     "sample_ms_default_shape": ms_default, "sample_ms_tuned": ms_tuned,
+                     "default_shape": "16384 points per tile, occupancy-limit CTAs per SM",
+                     "candidates": "points per tile 4096-65536 x CTAs per SM occupancy-1, "
+                                   "occupancy (10 shapes), timed on the sample"},
         "plain_per_instance": {"value": plain, "unit": "segments/s", "device_ms": pms,
                                "sample_instances": pinst,
                                "kernel": "plain_kernel: one thread per loop, points read "

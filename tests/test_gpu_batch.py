@@ -133,3 +133,56 @@ def test_plain_baseline_covers_the_lattice(setup):
     (gb, _, _), = ctx.batch_eval([{"handle": h, "field": fld, "cx": cx, "cy": cy, "T": T,
                                    "F": [1.0], "group": 128}])
     assert werr(g, gb) < W_TOL
+
+
+def test_batch_over_the_uneven_configuration_ranges_matches_oracle():
+    """Jobs drawn over the uneven-batch configuration's ranges (smooth,
+    Gaussian and lattice a = 5 lambda; spinor; F log-uniform in [0.01, 10];
+    lambda log-uniform in [0.1, 10]; ppl 512-8192; log-spaced T in
+    [1e-2, 1e2], rho in [0, 5 lambda]) on 256-loop ensembles (the oracle
+    evaluates them in seconds), in one batch: every checked (instance, F)
+    pair with F T' <= 10 (or F <= 0.1) within 1e-5 of max(|W64|, 1e-2 S);
+    beyond that, the error of the group mean below 1 % of its Monte Carlo
+    error bar and every group within 1e-2 (the FP32 phase limit stated with
+    the benchmark configuration)."""
+    import wltube
+
+    rng = np.random.default_rng(44)
+    ctx = wltube.Context(0)
+    try:
+        ens, jobs = {}, []
+        for k in range(9):
+            prof = ("smooth", "gaussian", "lattice")[k % 3]
+            F = float(np.exp(rng.uniform(np.log(0.01), np.log(10.0))))
+            lam = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
+            ppl = int(rng.choice([512, 1024, 2048, 4096, 8192]))
+            if prof == "lattice":  # keep the oracle's image sum small
+                ppl = min(ppl, 1024)
+            if ppl not in ens:
+                ens[ppl] = ctx.generate(4, 256, ppl)
+            nT, nrho = int(rng.integers(16, 65)), int(rng.integers(4, 9))
+            Tg = np.geomspace(1e-2, 1e2 if prof != "lattice" else 10.0, nT)
+            rho = np.linspace(0.0, 5.0 * lam, nrho)
+            cx, cy, T = f32_exact(np.repeat(rho, nT), np.zeros(nrho * nT), np.tile(Tg, nrho))
+            kw = {"tubedist": 5.0 * lam} if prof == "lattice" else {}
+            mode = 1 if prof == "lattice" else 0
+            jobs.append({"handle": ens[ppl], "ppl": ppl, "cx": cx, "cy": cy, "T": T, "F": [F],
+                         "group": 128,
+                         "field": wltube.field(prof, fermion=1, nint=4, lambda2=lam * lam, **kw),
+                         "ofield": O.field(prof, fermion=1, nint=4, mode=mode, lambda2=lam * lam,
+                                           **kw)})
+        outs = ctx.batch_eval(jobs, graph=True)
+        for j, (g, m, s) in zip(jobs, outs):
+            n = len(j["T"])
+            idx = np.unique(np.linspace(0, n - 1, 6).astype(int))
+            loops = ctx.download(j["handle"])
+            ref, S = O.eval_groups(loops, j["cx"][idx], j["cy"][idx], j["T"][idx], j["F"],
+                                   j["ofield"], return_scale=True)
+            acc = O.accuracy(g[idx], ref, S, j["F"], j["T"][idx])
+            if acc["max_rel_strict"] is not None:
+                assert acc["max_rel_strict"] <= W_TOL, (j["field"].profile, acc)
+            beyond = acc["max_err_over_sem_beyond_1e-5"]
+            assert beyond is None or beyond <= 1e-2, (j["field"].profile, acc)
+            assert acc["max_rel"] <= 1e-2, (j["field"].profile, acc)
+    finally:
+        ctx.close()

@@ -288,7 +288,7 @@ __device__ __noinline__ float4 lat_seg2_called(float2 uix, float2 uiy, float2 uj
 }
 
 // Lattice tile at 4 intervals with the images outer: two instances A, B per
-// thread (adjacent slots of the tile's instance order, 256 per CTA).  For
+// thread (slots t and t + 128 of the tile's instance order, 256 per CTA).  For
 // every staged chunk of a loop, the images of the two (loop, instance) pairs
 // walk all of the chunk's segments two at a time as packed f32x2 pairs:
 // A's image p beside B's image p while both have one, then the longer
@@ -299,8 +299,9 @@ __device__ __noinline__ float4 lat_seg2_called(float2 uix, float2 uiy, float2 uj
 // unit-loop points (reloaded from L2, the same address for every thread);
 // per image pair the walk is uniform across the warp (no per-segment image
 // loop, no row logic).  An instance's images are its range of image_range()
-// flattened row by row (k -> m0 + k / w, n0 + k % w); an unused half and
-// images outside the |R| disk are computed and not added.  Each image's walk
+// flattened row by row (k -> m0 + k / w, n0 + k % w), its rows trimmed to
+// the |R| disk where the range crosses it; an unused half is computed and
+// not added.  Each image's walk
 // over the chunk is summed in FP32 and added once, in image order, to its
 // instance's Kahan-compensated loop totals: an instance's sums do not depend
 // on its partner or on the tile's other instances.
@@ -316,7 +317,9 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
                                                float (*tot)[kSweepThreads], int *bad,
                                                float4 *ring, int &consumed) {
   const int tid = threadIdx.x;
-  const int sA = tile_x * kPairTile + 2 * tid, sB = sA + 1;
+  // slots t and t + 128: a tile holding 128 or fewer instances gives each
+  // thread at most one (the lanes of a warp still hold consecutive slots)
+  const int sA = tile_x * kPairTile + tid, sB = sA + kSweepThreads;
   const bool liveA = sA < A.ninst, liveB = sB < A.ninst;
   const int slA = liveA ? sA : A.ninst - 1, slB = liveB ? sB : A.ninst - 1;
   const int iA = A.perm ? A.perm[slA] : slA, iB = A.perm ? A.perm[slB] : slB;
@@ -338,7 +341,7 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
   if (tid == 0)
     for (int k = 0; k < K && k < kSweepStages; ++k) issue(k);
 #pragma unroll
-  for (int r = 0; r < kMaxF * 3; ++r) sacc[r][2 * tid] = sacc[r][2 * tid + 1] = 0.0;
+  for (int r = 0; r < kMaxF * 3; ++r) sacc[r][tid] = sacc[r][tid + kSweepThreads] = 0.0;
 
   const float2 il2 = f2(F.inv_l2);
   // loop totals per instance (h = 0: A, 1: B), Kahan-compensated, in tot[]
@@ -380,8 +383,29 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
     const ImgRange gA = image_range(bb, A.rtT[iA], A.cx[iA], A.cy[iA], F);
     const ImgRange gB = image_range(bb, A.rtT[iB], A.cx[iB], A.cy[iB], F);
     const int widA = max(gA.n1 - gA.n0 + 1, 1), widB = max(gB.n1 - gB.n0 + 1, 1);
-    const int nA = (gA.m1 >= gA.m0 && gA.n1 >= gA.n0) ? (gA.m1 - gA.m0 + 1) * widA : 0;
-    const int nB = (gB.m1 >= gB.m0 && gB.n1 >= gB.n0) ? (gB.m1 - gB.m0 + 1) * widB : 0;
+    // row m of a range trimmed to the disk m^2 + n^2 <= (rimage/a)^2 (the
+    // criterion image_range uses for `inside`)
+    auto row = [&](const ImgRange &g, int m, int &lo, int &hi) {
+      const float mm = (float)(m * m);
+      int nx = (int)floorf(sqrtf(fmaxf(F.rimg2 - mm, 0.0f)));
+      while (nx >= 0 && mm + (float)(nx * nx) > F.rimg2) --nx;
+      while (mm + (float)((nx + 1) * (nx + 1)) <= F.rimg2) ++nx;
+      lo = max(g.n0, -nx);
+      hi = min(g.n1, nx);
+    };
+    auto count = [&](const ImgRange &g, int wid) {
+      if (g.m1 < g.m0 || g.n1 < g.n0) return 0;
+      if (g.inside) return (g.m1 - g.m0 + 1) * wid;
+      int c = 0;
+      for (int m = g.m0; m <= g.m1; ++m) {
+        int lo, hi;
+        row(g, m, lo, hi);
+        c += max(hi - lo + 1, 0);
+      }
+      return c;
+    };
+    // a slot past the tile's instances walks nothing
+    const int nA = liveA ? count(gA, widA) : 0, nB = liveB ? count(gB, widB) : 0;
     const int mn = min(nA, nB), mx = max(nA, nB);
     const int steps = mn + (mx - mn + 1) / 2;
     const int qa = c == 0 ? 1 : (p0 >> 2), qend = p1 >> 2;
@@ -401,9 +425,26 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
       auto image = [&](int j, bool isB, bool &ok, float &s, float &crx, float &cry) {
         const ImgRange &g = isB ? gB : gA;
         const int wd = isB ? widB : widA, n = isB ? nB : nA;
-        const int jj = min(j, n - 1);
-        const int m = g.m0 + jj / wd, nn = g.n0 + jj % wd;
-        ok = j < n && (g.inside || (float)(m * m) + (float)(nn * nn) <= F.rimg2);
+        int jj = min(j, n - 1), m, nn;
+        if (g.inside) {
+          m = g.m0 + jj / wd;
+          nn = g.n0 + jj % wd;
+        } else {  // the rows trimmed to the disk, in order
+          m = g.m0;
+          nn = g.n0;
+          for (int mr = g.m0; mr <= g.m1; ++mr) {
+            int lo, hi;
+            row(g, mr, lo, hi);
+            const int cnt = max(hi - lo + 1, 0);
+            if (jj < cnt) {
+              m = mr;
+              nn = lo + jj;
+              break;
+            }
+            jj -= cnt;
+          }
+        }
+        ok = j < n;
         const int ic = isB ? iB : iA;
         s = A.rtT[ic];
         crx = fmaf(-(float)m, F.a, A.cx[ic]);
@@ -483,7 +524,7 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
     if (last) {
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {  // per-loop epilogue of each instance
-        const int ih = h ? iB : iA, col = 2 * tid + h;
+        const int ih = h ? iB : iA, col = tid + h * kSweepThreads;
         const df G[3] = {fast_two_sum(T(h, 0, 0), -T(h, 1, 0)),
                          fast_two_sum(T(h, 0, 1), -T(h, 1, 1)),
                          fast_two_sum(T(h, 0, 2), -T(h, 1, 2))};
@@ -517,8 +558,8 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
   consumed = base + K;
   for (int r = 0; r < A.nF * 3; ++r) {
     double *o = A.partial + ((size_t)chunk * A.nF * 3 + r) * A.ninst;
-    if (liveA) o[iA] = sacc[r][2 * tid];
-    if (liveB) o[iB] = sacc[r][2 * tid + 1];
+    if (liveA) o[iA] = sacc[r][tid];
+    if (liveB) o[iB] = sacc[r][tid + kSweepThreads];
   }
   return true;
 }
