@@ -264,6 +264,175 @@ struct Profile<kFixflux> : FixfluxProfile<false> {};
 template <>
 struct Profile<kFixfluxFF> : FixfluxProfile<true> {};
 
+// The fixflux profile with its Lentz continued fraction split out.  The
+// fraction (up to ~17 iterations of two divisions) is needed only where the
+// node lies in a bump region -- about a third of the nodes -- but on almost
+// every node some lane of a warp needs it, so evaluated in place the warp
+// runs ~16 iterations per node for an average lane need of ~3.  Instead the
+// fractions of a batch of nodes are gathered across the warp's lanes and
+// evaluated 32 at a time (a lane may evaluate another lane's), then each
+// lane finishes its own nodes in the usual order.
+//
+// fixflux_cf: whether the node at r2 needs a fraction, and its argument
+// -1/(1 - x^2) (x as phi_d / chi_d compute it)
+template <bool FF>
+__device__ __forceinline__ bool fixflux_cf(float r2, const FieldDev &F, float &arg) {
+  const float a = F.a;
+  float x;
+  if (r2 <= 0.25f * a * a) {
+    x = 2.0f * sqrtf(r2 * F.inv_l2);
+    if (!(x < (FF ? 1.0f : 0.999f))) return false;
+  } else {
+    const float rho = sqrtf(r2);
+    const float n = floorf((rho + 0.5f * a) / a);
+    x = 2.0f * (rho - n * a) / F.lam;
+    if (x <= (FF ? -1.0f : -0.999f) || !(x * x < (FF ? 1.0f : 0.999f))) return false;
+  }
+  arg = -1.0f / (1.0f - x * x);
+  return true;
+}
+
+// FixfluxProfile::eval with the node's fraction value E given (used only
+// where fixflux_cf says the node needs it)
+template <bool FF>
+__device__ __forceinline__ void fixflux_eval(float r2, const FieldDev &F, float E, float &g,
+                                             float &fp) {
+  const float a = F.a, lam = F.lam, lml = F.lml, aml = F.aml;
+  const float rho = sqrtf(r2);
+  const float n = floorf((rho + 0.5f * a) / a);
+  float f;
+  if (r2 <= 0.25f * a * a) {
+    const float x = 2.0f * sqrtf(r2 * F.inv_l2);
+    float phi = 1.0f;
+    if (x < (FF ? 1.0f : 0.999f)) {
+      const float onemx2 = 1.0f - x * x;
+      phi = 1.0f - (0.5f / 0.0742478f) * (onemx2 * expf(-1.0f / onemx2) + E);
+    }
+    f = (1.0f - 0.75f * lml) * phi + 3.0f * r2 / (a * a) * lml;
+  } else {
+    const float x = 2.0f * (rho - n * a) / lam;
+    const float onemx2 = 1.0f - x * x, x2 = x * x, x4 = x2 * x2;
+    float chi;
+    if (x <= (FF ? -1.0f : -0.999f)) {
+      chi = 0.0f;
+    } else if (x2 < (FF ? 1.0f : 0.999f)) {
+      chi = 0.5f * (-onemx2 * expf(-1.0f / onemx2) - E);
+      if (FF)
+        chi += 2.0f * n * a / lam *
+               (0.218f + 0.393f * x * coshf(0.806f * x4 - 0.696f * x2 + 0.0902f) /
+                             coshf(0.825f * x2 - 0.0234f * x + 0.375f));
+      else
+        chi += 2.0f * n * a / lam * 0.444f /
+               (1.0f + expf(-(3.31f * x + 5.25f * x * x2 * sinf(x) *
+                                              cosf(-0.907f * x2 - 1.29f * x4 * x4)) /
+                            cosf(x)));
+    } else {
+      chi = 2.0f * n * a * 0.443991f / lam;
+    }
+    f = 1.0f + 0.75f * (4.0f * r2 / (a * a) - 1.0f) * lml + 3.0f * n * (n - 1.0f) * aml;
+    f += 3.0f * lam / (0.443991f * a) * aml * chi;
+  }
+  g = f / r2;
+  const float bbg = 3.0f / (a * a) * lml;
+  if (rho <= 0.5f * a)
+    fp = bbg + 2.0f / (F.l2 * 0.0742478f) * (1.0f - 0.75f * lml) * bump_d(2.0f * rho / lam);
+  else
+    fp = bbg + 6.0f / (0.443991f * lam * a) * aml * bump_d(2.0f * (rho - n * a) / lam);
+}
+
+// nodes per gathering batch of the fixflux segment
+constexpr int kFfBatch = 8;
+constexpr int kFfWarps = 4;  // warps per CTA of the kernels that call it (128 threads)
+
+// segment<> for the fixflux profiles (run-time interval count), with the
+// continued fractions gathered per warp; the same node values and sums as
+// segment<> evaluating FixfluxProfile<FF>::eval node by node.  Not inlined:
+// one copy for the dozen call sites of the sweep.
+template <bool FF, bool FERM>
+__device__ __noinline__ float2 segment_fixflux(float zix, float ziy, float zjx, float zjy,
+                                               const FieldDev &F, float ph, float sp) {
+  __shared__ float cfq[kFfWarps][32 * kFfBatch];  // arguments, then values in place
+  __shared__ unsigned cfm[kFfWarps][kFfBatch];     // per node of the batch: lanes needing one
+  __shared__ int cfo[kFfWarps][kFfBatch];          // and their first queue slot
+  const int w = (threadIdx.x >> 5) & (kFfWarps - 1);
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __activemask();
+  const unsigned lt = (1u << lane) - 1u;
+  const int rank = __popc(act & lt), nact = __popc(act);
+  const bool leader = rank == 0;
+
+  const float dx = zjx - zix, dy = zjy - ziy;
+  float a = fmaf(zix, zix, ziy * ziy);
+  float b = fmaf(zix, dx, ziy * dy);
+  float c = fmaf(dx, dx, dy * dy);
+  const float xyyx = fmaf(zix, zjy, -(ziy * zjx));
+  a = fmaxf(a, F.clampA);
+  b = fmaxf(b, F.clampB);
+  c = fmaxf(c, F.clampC);
+  const float b2 = b + b;
+  const float as = a;
+  const float ae = fmaxf((as + b2) + c, F.clampE);
+  const int n = F.nint;
+  // node k of the evaluation order 0 (t = 0), n (t = 1), 1 .. n-1
+  auto node_j = [&](int k) { return k == 0 ? 0 : (k == 1 ? n : k - 1); };
+  auto node_r2 = [&](int j) {
+    if (j == 0) return as;
+    if (j == n) return ae;
+    const float t = (float)j * F.h;
+    return fmaxf(fmaf(fmaf(c, t, b2), t, as), F.clampI);
+  };
+  float g0 = 0.f, f0 = 0.f, g1 = 0.f, f1 = 0.f;
+  float so = 0.f, se = 0.f, fo = 0.f, fe = 0.f;
+  for (int k0 = 0; k0 <= n; k0 += kFfBatch) {
+    int base = 0;
+#pragma unroll
+    for (int kk = 0; kk < kFfBatch; ++kk) {  // gather the batch's fractions
+      const int k = k0 + kk;
+      if (k > n) break;
+      float arg = 0.0f;
+      const bool need = fixflux_cf<FF>(node_r2(node_j(k)), F, arg);
+      const unsigned m = __ballot_sync(act, need);
+      if (need) cfq[w][base + __popc(m & lt)] = arg;
+      if (leader) {
+        cfm[w][kk] = m;
+        cfo[w][kk] = base;
+      }
+      base += __popc(m);
+    }
+    __syncwarp(act);
+    for (int q = rank; q < base; q += nact) cfq[w][q] = expint_lentz(cfq[w][q]);
+    __syncwarp(act);
+#pragma unroll
+    for (int kk = 0; kk < kFfBatch; ++kk) {  // each lane's nodes, in order
+      const int k = k0 + kk;
+      if (k > n) break;
+      const int j = node_j(k);
+      const unsigned m = cfm[w][kk];
+      const float E = (m >> lane) & 1u ? cfq[w][cfo[w][kk] + __popc(m & lt)] : 0.0f;
+      float g, fp;
+      fixflux_eval<FF>(node_r2(j), F, E, g, fp);
+      if (j == 0) {
+        g0 = g;
+        f0 = fp;
+      } else if (j == n) {
+        g1 = g;
+        f1 = fp;
+      } else if (j & 1) {
+        so += g;
+        if (FERM) fo += fp;
+      } else {
+        se += g;
+        if (FERM) fe += fp;
+      }
+    }
+    __syncwarp(act);  // the queue is rewritten by the next batch
+  }
+  const float S = fmaf(4.0f, so, fmaf(2.0f, se, g0 + g1));
+  ph = fmaf(xyyx, S, ph);
+  if (FERM) sp += fmaf(4.0f, fo, fmaf(2.0f, fe, f0 + f1));
+  return make_float2(ph, sp);
+}
+
 // rho^2 shift folded into the segment polynomial (Profile<P>::shift where a
 // profile evaluates on l2 + rho^2, else 0)
 template <int P>
@@ -663,6 +832,11 @@ __device__ __forceinline__ void seg(float zix, float ziy, float zjx, float zjy,
                                     float &sp) {
   if constexpr (P == kLattice) {
     const float2 r = segment_lattice<FERM, NINT>(zix, ziy, zjx, zjy, F, img, ph, sp);
+    ph = r.x;
+    sp = r.y;
+  } else if constexpr ((P == kFixflux || P == kFixfluxFF) && NINT == 0) {
+    const float2 r =
+        segment_fixflux<P == kFixfluxFF, FERM>(zix, ziy, zjx, zjy, F, ph, sp);
     ph = r.x;
     sp = r.y;
   } else {

@@ -25,6 +25,10 @@
 
 namespace wl {
 
+// the fixflux segment's per-warp queues assume CTAs of kFfWarps warps
+static_assert(kSweepThreads == 32 * kFfWarps && kLoopWarps == kFfWarps,
+              "fixflux queues: 4 warps per CTA");
+
 // Shared-memory state of the sweep, reused by consecutive tiles of a CTA.
 struct SweepShared {
   uint64_t *full_bar;                  // [kSweepStages] mbarriers
