@@ -190,12 +190,17 @@ struct Profile<kPeriodic> {  // radial shells, intEV.cu:201-232 and 300-328
     const int i0 = (int)flraf - 2, i1 = (int)flraf + 2;
     float f = (i0 > 0) ? 0.5f * (flraf - 3.0f) * (flraf - 2.0f) : 0.0f;
     float d = 0.0f;
+    // The shell at the axis (i = 0, when i0 <= 0 <= i1) comes first in the
+    // loop's ascending order: it sets f and d, the shells i > 0 then add to
+    // them.  Evaluated before the loop, its exp and log run once per warp
+    // instead of once for each iteration at which some lane meets i = 0.
+    if (i0 <= 0) {
+      const float ex = expf(-rho / lam), ex1 = 1.0f + ex;
+      f = -rho / a * (ex / ex1) - lam / a * logf(ex1);
+      d = ex / (a * ex1 * ex1);
+    }
     for (int i = i0; i <= i1; i++) {
-      if (i == 0) {
-        const float ex = expf(-rho / lam), ex1 = 1.0f + ex;
-        f = -rho / a * (ex / ex1) - lam / a * logf(ex1);
-        d = ex / (a * ex1 * ex1);
-      } else if (i > 0) {
+      if (i > 0) {
         const float ea = expf(-(rho - (float)i * a) / lam), ea1 = 1.0f + ea;
         f = f + (float)i / ea1;
         d = d + ((float)i / rho) * ea / (ea1 * ea1);
