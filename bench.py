@@ -56,13 +56,15 @@ GROUP = 128
 # Algorithmic FP32 and MUFU operations per loop-segment of smooth spinor QED
 # at 5 Simpson nodes (fixed, not tuned).  MUFU: 5 reciprocals (f/rho^2 =
 # 1/(l2 + rho^2) at the two ends and three interior nodes; f' = l2 (f/rho^2)^2
-# needs none).  FP32: 38, the FP32 operations the kernel executes per
-# segment (ncu instruction mix: FFMA 21.2 + FADD 11.9 + FMUL 5.1): per
-# interior node 2 FMAs for rho^2, a square and 2 sums (15 for three nodes),
-# and the segment's set-up (point scaling, a, b, c, the cross term, the
-# polynomial's constants, the end squares, the Simpson combines); the clamps
-# run on the integer pipe.  No formulation with fewer is known here.
-ALG_FP32_PER_SEG = 38
+# needs none).  FP32: 34, the FP32 operations of the kernel's formula per
+# segment: the point scaling (2), z_j - z_i (2), a, b, c and the cross term
+# (2 each), the end values a + l2 and (a + l2 + 2b) + c (3), rho^2 at three
+# interior nodes (2 each), the phase's Simpson combine and product (5: the
+# sums open with their first node), the spin's squares fused into its sums
+# and their combine (8); the clamps run on the integer pipe, the blockwise
+# Kahan additions (0.75 per segment) are not counted.  No formulation with
+# fewer is known here.
+ALG_FP32_PER_SEG = 34
 ALG_MUFU_PER_SEG = 5
 # MUFU operations per loop-segment (lattice: per segment-image) of the
 # profiles of the uneven batch at 5 nodes: smooth 1 reciprocal per node;
@@ -1122,7 +1124,7 @@ def main():
         "W_evals_per_s": world * ninst * len(FLUX) / (ms_step * 1e-3),
         # the binding pipe is the MUFU (5 reciprocals per segment, exact for
         # the formula; 16 per SM per clock); the FP32 pipe is reported beside
-        # it with the 38 operations per segment the kernel executes
+        # it with the 34 operations of the segment's formula
         "roofline": {
             "bound": "mufu", "unit": "Gop/s",
             "achieved": mufu_ach / 1e9, "peak": mufu_peak / 1e9, "frac": mufu_ach / mufu_peak,

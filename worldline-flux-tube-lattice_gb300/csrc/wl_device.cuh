@@ -603,7 +603,7 @@ __device__ __forceinline__ void eval2(float2 r2, const FieldDev &F, float2 &g, f
 template <int P, bool FERM, int NINT>
 __device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, float2 zjy,
                                          const FieldDev &F, float2 &ph, float2 &sp) {
-  static_assert(!Profile<P>::kHeavy && NINT > 0, "pairs: light profiles, fixed intervals");
+  static_assert(!Profile<P>::kHeavy && NINT >= 4, "pairs: light profiles, fixed intervals");
   constexpr int kSoftRcp = soft_rcp_period<P, FERM, NINT, true>();
   const float2 dx = add2(zjx, neg2(zix)), dy = add2(zjy, neg2(ziy));
   float2 a = fma2(zix, zix, mul2(ziy, ziy));
@@ -613,17 +613,26 @@ __device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, flo
   a = max2(a, F.clampA);
   b = max2(b, F.clampB);
   c = max2(c, F.clampC);
-  const float2 b2 = add2(b, b);
   const float2 as = add2(a, f2(profile_shift<P>(F)));
-  const float2 ae = add2(add2(as, b2), c);
+  // (as + 2b) + c as the scalar segment rounds it: 2b is exact, so the fma
+  // rounds once as the sum does and 2b needs no register or operation
+  const float2 ae = add2(fma2(b, f2(2.0f), as), c);
   float2 g0, f0, g1, f1;
   eval2<P>(as, F, g0, f0);
   eval2<P>(ae, F, g1, f1);
-  float2 so = f2(0.0f), se = f2(0.0f), fo = f2(0.0f), fe = f2(0.0f);
+  // Simpson sums opened by their first node rather than by 0 + node, two
+  // operations fewer per sum.  The smooth profile's f' = g^2 enters its sums
+  // as explicit fma (the square of each later node fused into the running
+  // sum), so no sum of two products is left for the compiler to contract
+  // one way or the other.
+  constexpr bool kSq = (P == kSmooth);
+  float2 so, se, fo, fe;
 #pragma unroll
   for (int j = 1; j < NINT; j++) {
     const float t = (float)j * (1.0f / (float)NINT);
-    const float2 r2 = fma2(fma2(c, f2(t), b2), f2(t), as);
+    // as + t (2b + c t) = as + 2t (b + c t/2): halving and doubling are
+    // exact, so both fma round as the scalar segment's do
+    const float2 r2 = fma2(fma2(c, f2(0.5f * t), b), f2(2.0f * t), as);
     float2 g, fp;
     if (kSoftRcp > 0 && j % kSoftRcp == kSoftRcp - 1) {  // smooth only: g = 1/(l2 + rho^2)
       g = rcp_newton2(r2);
@@ -632,16 +641,19 @@ __device__ __forceinline__ void segment2(float2 zix, float2 ziy, float2 zjx, flo
       eval2<P>(r2, F, g, fp);
     }
     if (j & 1) {
-      so = add2(so, g);
-      if (FERM) fo = add2(fo, fp);
+      so = j == 1 ? g : add2(so, g);
+      if (FERM) fo = j == 1 ? (kSq ? mul2(g, g) : fp) : (kSq ? fma2(g, g, fo) : add2(fo, fp));
     } else {
-      se = add2(se, g);
-      if (FERM) fe = add2(fe, fp);
+      se = j == 2 ? g : add2(se, g);
+      if (FERM) fe = j == 2 ? (kSq ? mul2(g, g) : fp) : (kSq ? fma2(g, g, fe) : add2(fe, fp));
     }
   }
   const float2 S = fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(g0, g1)));
   ph = fma2(xyyx, S, ph);
-  if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(f0, f1))));
+  if (FERM) {
+    const float2 f01 = kSq ? fma2(g1, g1, mul2(g0, g0)) : add2(f0, f1);
+    sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, f01)));
+  }
 }
 
 // segment2 as a called function for many intervals: one copy of the long

@@ -237,16 +237,18 @@ __device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, flo
                                          float2 il2, float2 &ph, float2 &sp) {
   const float2 dx = add2(ujx, neg2(uix)), dy = add2(ujy, neg2(uiy));
   const float2 as = mul2(fma2(uix, uix, mul2(uiy, uiy)), il2);
-  const float2 bs2 = mul2(mul2(f2(2.0f), fma2(uix, dx, mul2(uiy, dy))), il2);
+  // b/l2 alone: 2b/l2, the linear coefficient, is its exact double, which
+  // the node polynomial takes through exact halvings and doublings of t
+  const float2 bs = mul2(fma2(uix, dx, mul2(uiy, dy)), il2);
   const float2 cs = mul2(fma2(dx, dx, mul2(dy, dy)), il2);
   const float2 cross = mul2(fma2(uix, dy, neg2(mul2(uiy, dx))), il2);
   float2 x[5];
   x[0] = as;
-  x[4] = add2(add2(as, bs2), cs);
+  x[4] = add2(fma2(bs, f2(2.0f), as), cs);  // (as + 2bs) + cs
 #pragma unroll
   for (int j = 1; j < 4; j++) {
     const float t = (float)j * 0.25f;
-    x[j] = fma2(fma2(cs, f2(t), bs2), f2(t), as);
+    x[j] = fma2(fma2(cs, f2(0.5f * t), bs), f2(2.0f * t), as);  // as + t (2bs + cs t)
   }
   float xmin = fminf(x[0].x, x[0].y);
 #pragma unroll
@@ -269,17 +271,9 @@ __device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, flo
     if (FERM)
       e[j] = make_float2(x[j].x > kLatFar ? 0.0f : e[j].x, x[j].y > kLatFar ? 0.0f : e[j].y);
   }
-  float2 so = f2(0.f), se = f2(0.f), fo = f2(0.f), fe = f2(0.f);
-  so = add2(so, q[1]);
-  se = add2(se, q[2]);
-  so = add2(so, q[3]);
-  if (FERM) {
-    fo = add2(fo, e[1]);
-    fe = add2(fe, e[2]);
-    fo = add2(fo, e[3]);
-  }
-  ph = fma2(cross, fma2(f2(4.0f), so, fma2(f2(2.0f), se, add2(q[0], q[4]))), ph);
-  if (FERM) sp = add2(sp, fma2(f2(4.0f), fo, fma2(f2(2.0f), fe, add2(e[0], e[4]))));
+  ph = fma2(cross, fma2(f2(4.0f), add2(q[1], q[3]), fma2(f2(2.0f), q[2], add2(q[0], q[4]))), ph);
+  if (FERM)
+    sp = add2(sp, fma2(f2(4.0f), add2(e[1], e[3]), fma2(f2(2.0f), e[2], add2(e[0], e[4]))));
 }
 
 // the rarely taken opening / closing segments as one called copy
