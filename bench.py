@@ -365,7 +365,7 @@ def c4_jobs(wltube, ctx, njobs, seed=4, profiles=("smooth", "gaussian")):
                                                                lambda2=lam * lam, **kw),
                      "profile": prof,
                      "cx": np.repeat(rho, nT), "cy": np.zeros(nrho * nT),
-                     "T": np.tile(T, nrho), "F": [F], "group": 128,
+                     "T": np.tile(T, nrho), "F": [F], "group": 128, "nT": nT,
                      "segments": Nl * ppl * nT * nrho})
     return jobs, ens
 
@@ -410,7 +410,7 @@ def single_instance_ms(ctx, job, idx):
     return total
 
 
-def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
+def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=16,
                   mufu_peak=None):
     """The uneven-batch configuration (seed 4): njobs jobs drawn from its
     distribution, autotuned, evaluated in one persistent graph-captured launch
@@ -441,19 +441,30 @@ def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
     st = ctx.batch_stats()
     bms = float(np.median(ms))
     batched = total / (bms * 1e-3)
-    # the per-instance denominators on the same sample of every job
-    psegs, pms, sms, pinst = 0, 0.0, 0.0, 0
+    # the per-instance denominators on a sample of every job, each job's
+    # sampled time scaled to its instance count: the time the per-instance
+    # path would take for this same batch (a job's instances cost alike up to
+    # their proper time, which the sample spreads over)
+    psegs, pms, sms, pinst, pest, sest = 0, 0.0, 0.0, 0, 0.0, 0.0
     for j in jobs:
-        n = len(j["T"])
-        idx = np.unique(np.linspace(0, n - 1, min(per_job_sample, n)).astype(int))
+        n, nT = len(j["T"]), j["nT"]
+        # stratified: proper times evenly over the job's log-spaced list (the
+        # cost of a lattice instance grows with T), centres over its rho list
+        m = min(per_job_sample, n)
+        it = np.linspace(0, nT - 1, m).round().astype(int)
+        ir = np.linspace(0, n // nT - 1, m).round().astype(int)[np.random.default_rng(m).permutation(m)]
+        idx = np.unique(ir * nT + it)
         _, _, _, t = ctx.eval_plain(j["handle"], j["field"], j["cx"][idx], j["cy"][idx],
                                     j["T"][idx], j["F"], j["group"])
+        ts = single_instance_ms(ctx, j, idx)
         pms += t
-        sms += single_instance_ms(ctx, j, idx)
+        sms += ts
+        pest += t * n / len(idx)
+        sest += ts * n / len(idx)
         psegs += j["segments"] // n * len(idx)
         pinst += len(idx)
-    plain = psegs / (pms * 1e-3)
-    single = psegs / (sms * 1e-3)
+    plain = total / (pest * 1e-3)
+    single = total / (sest * 1e-3)
     out = {
         "metric": "loop-segments/s (uneven batch, one persistent graph launch)",
         "value": batched, "unit": "segments/s", "ms_per_step": bms, "steps": steps,
@@ -464,17 +475,25 @@ def batch_measure(ctx, wltube, njobs, profiles, steps, warmup, per_job_sample=8,
                      "default_shape": "16384 points per tile, occupancy-limit CTAs per SM",
                      "candidates": "points per tile 4096-65536 x CTAs per SM occupancy-1, "
                                    "occupancy (10 shapes), timed on the sample"},
-        "plain_per_instance": {"value": plain, "unit": "segments/s", "device_ms": pms,
-                               "sample_instances": pinst,
+        "plain_per_instance": {"value": plain, "unit": "segments/s",
+                               "device_ms_batch_estimate": pest,
+                               "device_ms_sampled": pms, "sample_instances": pinst,
+                               "sample_rate": psegs / (pms * 1e-3),
                                "kernel": "plain_kernel: one thread per loop, points read "
                                          "from global memory (the reference kernel's "
                                          "structure), one launch per instance"},
-        "library_per_instance": {"value": single, "unit": "segments/s", "device_ms": sms,
-                                 "sample_instances": pinst,
+        "library_per_instance": {"value": single, "unit": "segments/s",
+                                 "device_ms_batch_estimate": sest,
+                                 "device_ms_sampled": sms, "sample_instances": pinst,
+                                 "sample_rate": psegs / (sms * 1e-3),
                                  "path": "wl_eval_device with one instance per call "
                                          "(loop-parallel kernel + reduction)"},
-        "speedup_vs_plain": batched / plain,
-        "speedup_vs_library_per_instance": batched / single,
+        "speedup_vs_plain": pest / bms,
+        "speedup_vs_library_per_instance": sest / bms,
+        "speedup_note": "per-instance time for this batch (each job's sampled device time x "
+                        "its instances / sampled instances) over the batch's device time; "
+                        "sample_rate is the per-instance path's rate on the sample alone, "
+                        "where every job weighs alike",
         "config": {"workload": "uneven batch drawn as the 512-instance configuration "
                                "(seed 4), %d jobs, profiles %s, spinor, 5 Simpson nodes, "
                                "F and lambda log-uniform, ppl 512-8192, Nl 1024-8192, "
