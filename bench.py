@@ -965,7 +965,7 @@ def main():
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
     ap.add_argument("--accuracy-instances", type=int, default=32,
                     help="timed instances the FP64 oracle checks (default line)")
-    ap.add_argument("--batch-jobs", type=int, default=16,
+    ap.add_argument("--batch-jobs", type=int, default=32,
                     help="jobs of the default line's uneven-batch sub-object (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=100,
                     help="requests per phase of the default line's serve sub-object (0: skip)")
