@@ -50,7 +50,8 @@ __device__ __forceinline__ void run_tile(int kprof, const SweepArgs &A, int tx, 
         break;
       case kLattice:
         if constexpr (NINT == 4)
-          sweep_tile_lat<FERM>(A, tx, chunk, S.full_bar, sacc2, tot, S.bad, S.ring, consumed);
+          sweep_tile_lat<FERM, false>(A, tx, chunk, S.full_bar, sacc2, tot, S.bad, S.ring,
+                                      consumed);
         break;
       default: break;
     }

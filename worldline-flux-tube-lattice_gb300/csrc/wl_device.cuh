@@ -729,6 +729,19 @@ __device__ __forceinline__ void gauss_q(float x, float &q, float &e) {
   q = x < 0.5f ? small : big;
 }
 
+// gauss_q2 where every x >= 0.5: the large-x form alone, without the small-x
+// polynomial.  The form is still taken through a select against a bound no
+// node reaches (x < neg1, the caller passing -1 as a run-time value): so
+// written, a walk's sums are bit-identical to gauss_q2's on the lattice
+// parity cases; with the product returned directly they were not (measured
+// on the GB300; the cause was not found in the source), and the lattice
+// kernel needs the two walks to agree bit for bit.
+__device__ __forceinline__ void gauss_q2_big(float2 x, float2 &q, float2 &e, float neg1) {
+  const float2 a = mul2(f2(-1.4426950408889634f), x);
+  e = make_float2(ex2_fast(a.x), ex2_fast(a.y));
+  const float2 big = mul2(add2(f2(1.0f), neg2(e)), rcp2(x));
+  q = make_float2(x.x < neg1 ? 0.0f : big.x, x.y < neg1 ? 0.0f : big.y);
+}
 // gauss_q on a pair (each half as gauss_q)
 __device__ __forceinline__ void gauss_q2(float2 x, float2 &q, float2 &e) {
   const float2 a = mul2(f2(-1.4426950408889634f), x);

@@ -233,7 +233,7 @@ constexpr int kPairTile = 2 * kSweepThreads;
 // over blocks of staged points decide once per block instead (kLatSub).
 constexpr float kLatFar = 18.0f;
 
-template <bool FERM, bool VOTE = true>
+template <bool FERM, bool VOTE = true, bool MID = false>
 __device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, float2 ujy,
                                          float2 il2, float2 &ph, float2 &sp) {
   const float2 dx = add2(ujx, neg2(uix)), dy = add2(ujy, neg2(uiy));
@@ -268,7 +268,10 @@ __device__ __forceinline__ void lat_seg2(float2 uix, float2 uiy, float2 ujx, flo
   float2 q[5], e[5];
 #pragma unroll
   for (int j = 0; j < 5; j++) {
-    gauss_q2(x[j], q[j], e[j]);
+    if (MID)  // every node at x >= 0.5 (the caller's block test); il2 > 0
+      gauss_q2_big(x[j], q[j], e[j], il2.x < 0.0f ? 1.0f : -1.0f);
+    else
+      gauss_q2(x[j], q[j], e[j]);
     if (FERM)
       e[j] = make_float2(x[j].x > kLatFar ? 0.0f : e[j].x, x[j].y > kLatFar ? 0.0f : e[j].y);
   }
@@ -312,6 +315,10 @@ __device__ __forceinline__ void lat_seg2_far(float2 uix, float2 uiy, float2 ujx,
 // 11-13 % faster; boxes of 64, 128, 256 points 0.5-3 % slower than 32; the
 // near walk with the vote kept 4-9 % slower; unrolled by 4, 4-25 % slower.
 constexpr float kLatFarChunk = 19.0f;
+// A block whose box stays at x > 0.55 from the image centres has every node
+// at x >= 0.5 (the same margin argument), where the integrand takes its
+// large-x form: the walk skips the small-x polynomial and its selects.
+constexpr float kLatMidChunk = 0.55f;
 constexpr int kLatSub = 32;  // staged points per far-test box
 constexpr int kLatNSub = kSweepChunkPts / kLatSub;
 static_assert(kSweepChunkPts % kLatSub == 0 && kLatSub % 4 == 0, "whole groups per box");
@@ -349,7 +356,11 @@ __device__ __noinline__ float4 lat_seg2_called(float2 uix, float2 uiy, float2 uj
 // of registers: they are touched once per image walk)
 constexpr int kLatTotRows = 2 * 4 * 3;
 
-template <bool FERM>
+// MIDWALK: walk the blocks between near and far with the large-x form alone
+// (the single-job kernel; inside the persistent batch kernel the extra walk
+// measured 3 % slower on the uneven batch, so its tiles keep two walks --
+// the sums are the same bits either way)
+template <bool FERM, bool MIDWALK>
 __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, int chunk,
                                                uint64_t *full_bar, double (*sacc)[kPairTile],
                                                float (*tot)[kSweepThreads], int *bad,
@@ -448,12 +459,12 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
     }
     // the nearest point of block b's box, scaled and shifted as U() maps the
     // points (fma(s, w, c - R) is monotone in w), is far from the image centre
-    auto block_far = [&](int b, float sc, float crx, float cry) {
+    auto block_x = [&](int b, float sc, float crx, float cry) {
       const float4 bb = lat_box[tid >> 5][b];
       const float lx = fmaf(sc, bb.x, crx), hx = fmaf(sc, bb.y, crx);
       const float ly = fmaf(sc, bb.z, cry), hy = fmaf(sc, bb.w, cry);
       const float ex = fmaxf(fmaxf(lx, -hx), 0.0f), ey = fmaxf(fmaxf(ly, -hy), 0.0f);
-      return fmaf(ex, ex, ey * ey) * F.inv_l2 > kLatFarChunk;
+      return fmaf(ex, ex, ey * ey) * F.inv_l2;
     };
     // this loop's images of each instance
     const float4 bb = A.bbox[l];
@@ -574,6 +585,9 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
       auto far_seg = [&](float2 ix, float2 iy, float2 jx, float2 jy, int r) {
         lat_seg2_far(ix, iy, jx, jy, il2, bp[r]);
       };
+      auto mid_seg = [&](float2 ix, float2 iy, float2 jx, float2 jy, int r) {
+        lat_seg2<FERM, false, true>(ix, iy, jx, jy, il2, bp[r], bs[r]);
+      };
       auto near_seg = [&](float2 ix, float2 iy, float2 jx, float2 jy, int r) {
         lat_seg2<FERM, false>(ix, iy, jx, jy, il2, bp[r], bs[r]);
       };
@@ -582,12 +596,18 @@ __device__ __forceinline__ bool sweep_tile_lat(const SweepArgs &A, int tile_x, i
         const int q0 = max(qa, (p0 + b * kLatSub) >> 2);
         const int q1 = min(qend, (p0 + (b + 1) * kLatSub) >> 2);
         // an unused half is not added: it never holds the warp back
-        const bool far = (!okx || block_far(b, sx, cxx, cyx)) && (!oky || block_far(b, sy, cxy, cyy));
-        if (__all_sync(__activemask(), far)) {
+        const float xb = fminf(okx ? block_x(b, sx, cxx, cyx) : INFINITY,
+                               oky ? block_x(b, sy, cxy, cyy) : INFINITY);
+        const unsigned am = __activemask();
+        if (__all_sync(am, xb > kLatFarChunk)) {
           // every node of the block's walk is far: reciprocals only, no
           // per-segment vote, four segments of straight-line work per group
 #pragma unroll 2
           for (int q = q0; q < q1; ++q) group4(q, far_seg);
+        } else if (MIDWALK && __all_sync(am, xb > kLatMidChunk)) {
+          // no node near an image centre: the integrand's large-x form alone
+#pragma unroll 2
+          for (int q = q0; q < q1; ++q) group4(q, mid_seg);
         } else {
 #pragma unroll 2
           for (int q = q0; q < q1; ++q) group4(q, near_seg);
@@ -865,7 +885,8 @@ __global__ void __launch_bounds__(kSweepThreads, 4)
   }
   __syncthreads();
   int consumed = 0;
-  sweep_tile_lat<FERM>(A, blockIdx.x, blockIdx.y, full_bar, sacc, tot, &sm_bad, ring, consumed);
+  sweep_tile_lat<FERM, true>(A, blockIdx.x, blockIdx.y, full_bar, sacc, tot, &sm_bad, ring,
+                             consumed);
 }
 
 template <int P, bool FERM, int NINT>
