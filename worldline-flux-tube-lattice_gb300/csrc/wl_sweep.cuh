@@ -231,6 +231,8 @@ constexpr int kPairTile = 2 * kSweepThreads;
 // of the small-x polynomial -- with results bit-identical to the full path,
 // so an instance's sums still do not depend on its warp-mates.  The walks
 // over blocks of staged points decide once per block instead (kLatSub).
+// With MID the caller knows every node is at x >= 0.5: the integrand's
+// large-x form alone (gauss_q2_big), the same bits as gauss_q2 there.
 constexpr float kLatFar = 18.0f;
 
 template <bool FERM, bool VOTE = true, bool MID = false>
