@@ -7,7 +7,9 @@
 #   oracle/build_ref.sh [REFERENCE_DIR]      (default /root/reference)
 #
 # Outputs oracle/_ref/ref_driver_<profile> for the intEV.cu profiles and
-# oracle/_ref/ref_driver_ff for intEVff.cu (fixflux, spinor), and the GPU
+# oracle/_ref/ref_driver_ff for intEVff.cu (fixflux, spinor),
+# oracle/_ref/ref_spline (periodic.c's spline table with the GSL ODE
+# stand-in of refshim/), and the GPU
 # kernels oracle/_ref/ref_<case>.cubin (sm_103a device code of intEV.cu /
 # intEVff.cu with the reference's own -prec-div=false -prec-sqrt=false).  Exits 0 without
 # building when the reference tree is absent.
@@ -47,7 +49,17 @@ build_cubin() {  # name, kernel source, profile, lattice spacing, extra defines
     -DWLREF_TUBEDIST=${a}f $extra $SHIM "$REF/$src" -o "$OUT/ref_$name.cubin"
 }
 
+# the spline-profile table builder (periodic.c) with the GSL ODE stand-in
+build_spline() {
+  local o="$OUT/obj/spline"
+  "$CC" -c $CFLAGS "$REF/periodic.c" -o "$o.periodic.o"
+  "$CC" -c $CFLAGS "$HERE/refshim/gsl_odeiv2_standin.c" -o "$o.gsl.o"
+  "$CC" -c $CFLAGS "$HERE/ref_spline.c" -o "$o.driver.o"
+  "$CC" -o "$OUT/ref_spline" "$o.driver.o" "$o.periodic.o" "$o.gsl.o" -lm
+}
+
 pids=()
+build_spline & pids+=($!)
 for prof in step smooth quadratic gaussian; do
   build_cubin "$prof" intEV.cu "$prof" 1.0 "" & pids+=($!)
 done

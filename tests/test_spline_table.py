@@ -1,9 +1,8 @@
 """The spline profile's table (no GPU): the library's host builder
 (wl_spline_table: Gauss-Legendre per knot interval, clamped cubic spline in
 rho^2) against the oracle's independent restatement (composite Simpson,
-second-derivative spline form).  The reference builds the table with GSL's
-ODE stepper (periodic.c:113-164), absent here: parity of this profile is
-unpinned against the reference itself."""
+second-derivative spline form).  Both against the reference's own table
+builder (periodic.c:113-164 with a GSL stand-in): test_spline_reference.py."""
 import os
 import sys
 

@@ -32,8 +32,12 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # is not affected by these options.  The spline profile keeps IEEE division
 # and square root (with the approximate ones a spinor case moved to 1.05e-5
 # of the FP64 oracle, above the 1e-5 tolerance, for a 1.2x gain).
+# The spline table is built on the host in FP64 with every operation rounded
+# on its own (no fused multiply-add, which Arm hosts would otherwise contract
+# and x86 hosts not), so that it is the same table on every host.
 EXTRA_FLAGS = {"wl_sweep_periodic.cu": ["-prec-div=false", "-prec-sqrt=false"],
-               "wl_sweep_fixflux.cu": ["-prec-div=false", "-prec-sqrt=false"]}
+               "wl_sweep_fixflux.cu": ["-prec-div=false", "-prec-sqrt=false"],
+               "wl_spline.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 SOURCES = ["wl_sweep_smooth.cu", "wl_sweep_simple.cu", "wl_sweep_periodic.cu",
            "wl_sweep_lattice.cu", "wl_sweep_spline.cu",
            "wl_sweep_fixflux.cu", "wl_misc.cu", "wl_api.cpp", "wl_noalloc.cu",

@@ -52,7 +52,7 @@ int spline_table(double lambda2, double a, int n, float *rho2, float *coef4) {
     const double sn = sin(M_PI * s / a);
     return 2.0 / lambda2 * s * exp(-sn * sn / lambda2);
   };
-  std::vector<double> f(n), x(n);
+  std::vector<double> f(n);
   double acc = 0.0;
   for (int i = 0; i < n; ++i) {  // step [i h, (i + 1) h]
     const double lo = i * h, mid = lo + 0.5 * h;
@@ -62,14 +62,18 @@ int spline_table(double lambda2, double a, int n, float *rho2, float *coef4) {
     f[i] = acc;
     const double r = (i + 1) * h;
     rho2[i] = (float)(r * r);
-    x[i] = (double)rho2[i];
   }
-  // clamped cubic spline in x = rho^2 with zero end slopes: S_i(x) = f_i +
+  // clamped cubic spline in x = rho^2 with zero end slopes (Burden and
+  // Faires, algorithm 3.5, as periodic.c:46-110 applies it): S_i(x) = f_i +
   // b_i d + c_i d^2 + d_i d^3, d = x - x_i; c from the tridiagonal system of
-  // slope continuity, solved by Gaussian elimination without pivoting (the
-  // matrix is diagonally dominant)
-  std::vector<double> hh(n - 1), alpha(n), l(n), mu(n), z(n), c(n), b(n - 1), d(n - 1);
-  for (int i = 0; i < n - 1; ++i) hh[i] = x[i + 1] - x[i];
+  // slope continuity (Crout factorisation).  The knot differences are taken
+  // in FP32 as the reference takes them from its float knots, and each c_i
+  // is rounded to FP32 before the next row and b_i, d_i use it (the
+  // reference back-substitutes through its float table); so the table
+  // matches the reference's bit for bit (tests/test_spline_reference.py).
+  std::vector<double> hh(n - 1), alpha(n), l(n), mu(n), z(n);
+  std::vector<float> c(n);
+  for (int i = 0; i < n - 1; ++i) hh[i] = (double)(rho2[i + 1] - rho2[i]);
   alpha[0] = 3.0 * (f[1] - f[0]) / hh[0];
   alpha[n - 1] = -3.0 * (f[n - 1] - f[n - 2]) / hh[n - 2];
   for (int i = 1; i < n - 1; ++i)
@@ -78,23 +82,24 @@ int spline_table(double lambda2, double a, int n, float *rho2, float *coef4) {
   mu[0] = 0.5;
   z[0] = alpha[0] / l[0];
   for (int i = 1; i < n - 1; ++i) {
-    l[i] = 2.0 * (x[i + 1] - x[i - 1]) - hh[i - 1] * mu[i - 1];
+    l[i] = 2.0 * (double)(rho2[i + 1] - rho2[i - 1]) - hh[i - 1] * mu[i - 1];
     mu[i] = hh[i] / l[i];
     z[i] = (alpha[i] - hh[i - 1] * z[i - 1]) / l[i];
   }
   l[n - 1] = hh[n - 2] * (2.0 - mu[n - 2]);
   z[n - 1] = (alpha[n - 1] - hh[n - 2] * z[n - 2]) / l[n - 1];
-  c[n - 1] = z[n - 1];
+  c[n - 1] = (float)z[n - 1];
+  coef4[4 * (n - 1)] = (float)f[n - 1];
+  coef4[4 * (n - 1) + 1] = 0.0f;
+  coef4[4 * (n - 1) + 2] = c[n - 1];
+  coef4[4 * (n - 1) + 3] = 0.0f;
   for (int i = n - 2; i >= 0; --i) {
-    c[i] = z[i] - mu[i] * c[i + 1];
-    b[i] = (f[i + 1] - f[i]) / hh[i] - hh[i] * (c[i + 1] + 2.0 * c[i]) / 3.0;
-    d[i] = (c[i + 1] - c[i]) / (3.0 * hh[i]);
-  }
-  for (int i = 0; i < n; ++i) {
+    c[i] = (float)(z[i] - mu[i] * (double)c[i + 1]);
     coef4[4 * i] = (float)f[i];
-    coef4[4 * i + 1] = i < n - 1 ? (float)b[i] : 0.0f;
-    coef4[4 * i + 2] = (float)c[i];
-    coef4[4 * i + 3] = i < n - 1 ? (float)d[i] : 0.0f;
+    coef4[4 * i + 1] =
+        (float)((f[i + 1] - f[i]) / hh[i] - hh[i] * ((double)c[i + 1] + 2.0 * (double)c[i]) / 3.0);
+    coef4[4 * i + 2] = c[i];
+    coef4[4 * i + 3] = (float)(((double)c[i + 1] - (double)c[i]) / (3.0 * hh[i]));
   }
   return 0;
 }
