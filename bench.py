@@ -750,18 +750,18 @@ def lattice_node_stats(loops, cx, cy, T, a, lam, rimage, far=18.0):
     return nimg / pairs, (near / nodes if nodes else 0.0)
 
 
-def run_lattice(args):
+def lattice_measure(cases_spec, ngrid=32, tstride=12):
     """Square lattice of Gaussian tubes (lambda = 1, F = 1, images to 12a):
-    Nl = 8192 x ppl = 4096 (seed 3), the configuration's 32 x 32 grid of
-    centres over one unit cell at every 12th of its 96 log-spaced T in
-    [1e-2, 1e2] (8 T: the whole grid would take ~10 min per case), a in
-    {2, 5, 10}, scalar and spinor; one timed evaluation per case after a
-    warm-up."""
+    Nl = 8192 x ppl = 4096 (seed 3), the configuration's ngrid x ngrid grid of
+    centres over one unit cell at every tstride-th of its 96 log-spaced T in
+    [1e-2, 1e2] (8 T at tstride 12: the whole grid would take ~10 min per
+    case), for the (a, fermion) cases "a:fe,a:fe"; one timed evaluation per
+    case after a warm-up.  Returns the JSON object."""
     import torch
 
     import wltube
 
-    Nl, ppl, seed, ngrid = 8192, 4096, 3, args.lattice_grid
+    Nl, ppl, seed = 8192, 4096, 3
     ctx = wltube.Context(0)
     h = ctx.generate(seed, Nl, ppl)
     host = ctx.download(h)
@@ -769,12 +769,12 @@ def run_lattice(args):
                      host[:, :, 1].min(1), host[:, :, 1].max(1)], axis=1)
     host_sample = host[::1024].copy()
     del host
-    Tg = np.geomspace(1e-2, 1e2, 96)[args.lattice_tstride // 2::args.lattice_tstride]
+    Tg = np.geomspace(1e-2, 1e2, 96)[tstride // 2::tstride]
     nT = len(Tg)
     stream = torch.cuda.ExternalStream(ctx.stream())
     mufu_peak = ctx.peak_probe(1)
     cases = []
-    wanted = [(float(c.split(":")[0]), int(c.split(":")[1])) for c in args.lattice_cases.split(",")]
+    wanted = [(float(c.split(":")[0]), int(c.split(":")[1])) for c in cases_spec.split(",")]
     for a in sorted({a for a, _ in wanted}):
         u = (np.arange(ngrid) + 0.5) / ngrid * a
         gx, gy = np.meshgrid(u, u, indexing="ij")
@@ -823,7 +823,9 @@ def run_lattice(args):
                               seg_img / (ms * 1e-3) * ALG_MUFU_PER_SEG_IMAGE / mufu_peak,
                           "W_mean_sample": float(dm[n // 2].item()), "clocks": clk})
             sys.stderr.write("lattice a=%g fermion=%d: %.0f ms\n" % (a, fe, ms))
-    print(json.dumps({
+    ctx.release(h)
+    ctx.close()
+    return {
         "metric": "lattice: loop-segments/s and segment-image evaluations/s",
         "value": float(np.sum([c["instances"] * Nl * ppl for c in cases]) /
                        (np.sum([c["ms"] for c in cases]) * 1e-3)),
@@ -839,9 +841,13 @@ def run_lattice(args):
                                "|R|<=12a, Nl=8192 x ppl=4096 (seed 3), %d of the 96 log T in "
                                "[1e-2,1e2] (every %dth), %dx%d centres over one unit cell, "
                                "(a, fermion) in %s, 5 Simpson nodes, exact mode"
-                               % (nT, args.lattice_tstride, ngrid, ngrid, args.lattice_cases)}}))
-    ctx.release(h)
-    ctx.close()
+                               % (nT, tstride, ngrid, ngrid, cases_spec)}}
+
+
+def run_lattice(args):
+    """The square-lattice configuration on its own (one JSON line)."""
+    print(json.dumps(lattice_measure(args.lattice_cases, args.lattice_grid,
+                                     args.lattice_tstride)))
 
 
 def effact_legacy(ctx, h, Nl, ppl, l2, F, nrho, panels):
@@ -965,6 +971,9 @@ def main():
     ap.add_argument("--requests", type=int, default=150, help="requests per serve phase")
     ap.add_argument("--accuracy-instances", type=int, default=32,
                     help="timed instances the FP64 oracle checks (default line)")
+    ap.add_argument("--lattice-line-cases", default="10:0,5:1",
+                    help="(a, fermion) cases of the default line's lattice sub-object "
+                         "('' to skip)")
     ap.add_argument("--batch-jobs", type=int, default=32,
                     help="jobs of the default line's uneven-batch sub-object (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=100,
@@ -1140,8 +1149,15 @@ def main():
                "device_ms": ms50, "instances": len(sT), "simpson_intervals": 50,
                "note": "the same instances, loops and interval count as the reference arm's "
                        "gpu_kernel (its ExpectValue on this GPU)"}
-    batch = serve = None
+    batch = serve = lattice = None
     if rank == 0 and world == 1 and not args.small:
+        if args.lattice_line_cases:
+            # the square-lattice configuration on a few of its cases; a
+            # failure here is reported in the sub-object, not in the line
+            try:
+                lattice = lattice_measure(args.lattice_line_cases)
+            except Exception as e:  # noqa: BLE001
+                lattice = {"unavailable": "%s: %s" % (type(e).__name__, e)}
         if args.batch_jobs > 0:
             batch = batch_measure(ctx, wltube, args.batch_jobs,
                                   tuple(args.batch_profiles.split(",")), steps=1, warmup=1,
@@ -1192,7 +1208,7 @@ def main():
         },
         "accuracy": acc,
         "e2e": e2e, "L_eff_sample": leff_summary, "cpu_baseline": cpu,
-        "batch": batch, "serve": serve, "n50_same_instances": n50,
+        "batch": batch, "serve": serve, "lattice": lattice, "n50_same_instances": n50,
         "gpu_launches": launches, "clocks": clk,
     }
     print(json.dumps(line))
